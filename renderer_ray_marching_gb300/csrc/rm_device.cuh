@@ -1,0 +1,306 @@
+// rm_device.cuh -- device-side building blocks shared by the index, radii,
+// marcher and backward kernels.
+//
+// Floating-point contract.  Every operation whose rounding decides a result
+// bit is written with an explicit round-to-nearest intrinsic so that the
+// compiler cannot contract differently from the reference's GPU build:
+//   d2(c, q) = fma(dz, dz, fma(dx, dx, dy*dy)), d = c - q
+//       FLANN CudaL2::dist (third_party/flann/algorithms/kdtree_cuda_3d_index.cu:186-192,
+//       dot(float4) of util/cutil_math.h:1127-1130 with w = 0) as nvcc contracts it;
+//   p(t) = fma(dir, t, o)                    src/ray_marching.cu:216
+//   dot3(a, b) = fma(az, bz, fma(ax, bx, ay*by))      src/ray_marching.cu:78-79
+//   mat*vec row = fma(c0, x, c1*y) + fma(c2, z, c3*w) glm column sum, :77
+//   |v|^2 = fma(x, x, y*y) + fma(z, z, w*w); normalize = v * (1 / sqrt(|v|^2))
+// The same expressions are in the CPU oracle, compiled without contraction.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rm {
+
+constexpr int KNN = 10;             // src/ray_marching.h:17
+constexpr float ZFAR = 100.0f;      // src/common.h:4
+constexpr float ZNEAR = 0.1f;       // src/common.h:5
+constexpr int MAX_STEPS = 128;      // src/common.h:6
+constexpr float MIN_DIST = 0.001f;  // src/common.h:7
+constexpr int MAX_LEVELS = 14;      // 4^14 leaf slots
+constexpr int STACK = 3 * MAX_LEVELS + 4;
+constexpr int GROUP_F4 = 8;         // float4 per child group (6 used)
+
+// Index view passed by value to kernels.
+struct IndexDev {
+  const float4* rec;     // sorted records (x, y, z, radius)
+  const float4* col;     // sorted colours (r, g, b, 1)
+  const float4* groups;  // child groups: per internal node, its 4 children's boxes
+  const int32_t* perm;   // sorted position -> cloud index
+  int64_t n;             // points
+  int32_t leaf;          // points per leaf
+  int32_t depth;         // level of the leaves (>= 1); the root is level 0
+};
+
+// Offset of the first child group of level `lvl` (levels 0..depth-1 own groups).
+__host__ __device__ __forceinline__ int64_t group_offset(int lvl) {
+  return (int64_t)(((1ull << (2 * lvl)) - 1ull) / 3ull);
+}
+
+__device__ __forceinline__ float d2_point(float4 c, float qx, float qy, float qz) {
+  float dx = __fsub_rn(c.x, qx);
+  float dy = __fsub_rn(c.y, qy);
+  float dz = __fsub_rn(c.z, qz);
+  return __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+}
+
+// Lower bound of d2_point over a box: each axis gap is fl(|c - q|) of the
+// nearest face, which never exceeds fl(|c - q|) for a contained c because
+// rounding is monotone; the same fma chain keeps the bound monotone.
+__device__ __forceinline__ float d2_box(float lx, float ly, float lz, float hx, float hy,
+                                        float hz, float qx, float qy, float qz) {
+  float gx = fmaxf(fmaxf(__fsub_rn(lx, qx), __fsub_rn(qx, hx)), 0.0f);
+  float gy = fmaxf(fmaxf(__fsub_rn(ly, qy), __fsub_rn(qy, hy)), 0.0f);
+  float gz = fmaxf(fmaxf(__fsub_rn(lz, qz), __fsub_rn(qz, hz)), 0.0f);
+  return __fmaf_rn(gz, gz, __fmaf_rn(gx, gx, __fmul_rn(gy, gy)));
+}
+
+// k nearest candidates kept sorted by (d2, cloud index) ascending.
+template <int K>
+struct KList {
+  float d[K];
+  int32_t s[K];   // sorted position, -1 = empty
+  float r[K];     // record .w (radius)
+};
+
+template <int K>
+__device__ __forceinline__ void klist_init(KList<K>& L) {
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    L.d[j] = __int_as_float(0x7f800000);
+    L.s[j] = -1;
+    L.r[j] = 0.0f;
+  }
+}
+
+// (d, s) before (dj, sj)?  Equal distances compare cloud indices (rare path).
+__device__ __forceinline__ bool knn_before(float d, int32_t s, float dj, int32_t sj,
+                                           const int32_t* __restrict__ perm) {
+  if (d < dj) return true;
+  if (!(d == dj) || sj < 0) return false;
+  return __ldg(perm + s) < __ldg(perm + sj);
+}
+
+template <int K>
+__device__ __forceinline__ void klist_insert(KList<K>& L, float d, int32_t s, float r,
+                                             const int32_t* __restrict__ perm) {
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    if (knn_before(d, s, L.d[j], L.s[j], perm)) {
+      float td = L.d[j];
+      int32_t ts = L.s[j];
+      float tr = L.r[j];
+      L.d[j] = d;
+      L.s[j] = s;
+      L.r[j] = r;
+      d = td;
+      s = ts;
+      r = tr;
+    }
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void scan_leaf(const IndexDev& ix, int64_t leaf, float qx, float qy,
+                                          float qz, KList<K>& L) {
+  int64_t start = leaf * ix.leaf;
+  int64_t end = start + ix.leaf;
+  if (end > ix.n) end = ix.n;
+  for (int64_t i = start; i < end; ++i) {
+    float4 c = __ldg(ix.rec + i);
+    float d = d2_point(c, qx, qy, qz);
+    if (d <= L.d[K - 1]) klist_insert<K>(L, d, (int32_t)i, c.w, ix.perm);
+  }
+}
+
+#define RM_CSWAP(ma, ca, mb, cb)              \
+  do {                                        \
+    if ((mb) < (ma)) {                        \
+      float _tm = (ma); (ma) = (mb); (mb) = _tm; \
+      int _tc = (ca); (ca) = (cb); (cb) = _tc;   \
+    }                                         \
+  } while (0)
+
+// Exact k-NN over the implicit 4-ary tree.  A subtree is expanded whenever
+// its box bound is <= the current k-th distance, so equal-distance points
+// with a lower index are never skipped.  Returns false only if the stack
+// bound was exceeded (cannot happen for depth <= MAX_LEVELS).
+template <int K>
+__device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, KList<K>& L) {
+  klist_init<K>(L);
+  if (ix.n <= 0) return true;
+  uint32_t stk[STACK];
+  float stkd[STACK];
+  int sp = 0;
+  int lvl = 0;
+  uint32_t j = 0;
+  while (true) {
+    const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
+    float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
+    float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
+    float m0 = d2_box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, qx, qy, qz);
+    float m1 = d2_box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, qx, qy, qz);
+    float m2 = d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz);
+    float m3 = d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz);
+    int c0 = 0, c1 = 1, c2 = 2, c3 = 3;
+    RM_CSWAP(m0, c0, m1, c1);
+    RM_CSWAP(m2, c2, m3, c3);
+    RM_CSWAP(m0, c0, m2, c2);
+    RM_CSWAP(m1, c1, m3, c3);
+    RM_CSWAP(m1, c1, m2, c2);
+    uint32_t base = j * 4u;
+    if (lvl + 1 == ix.depth) {
+      if (m0 <= L.d[K - 1]) {
+        scan_leaf<K>(ix, base + c0, qx, qy, qz, L);
+        if (m1 <= L.d[K - 1]) {
+          scan_leaf<K>(ix, base + c1, qx, qy, qz, L);
+          if (m2 <= L.d[K - 1]) {
+            scan_leaf<K>(ix, base + c2, qx, qy, qz, L);
+            if (m3 <= L.d[K - 1]) scan_leaf<K>(ix, base + c3, qx, qy, qz, L);
+          }
+        }
+      }
+    } else {
+      float w = L.d[K - 1];
+      if (sp + 3 > STACK) return false;
+      uint32_t code = (uint32_t)(lvl + 1) << 28;
+      if (m3 <= w) { stk[sp] = code | (base + c3); stkd[sp] = m3; ++sp; }
+      if (m2 <= w) { stk[sp] = code | (base + c2); stkd[sp] = m2; ++sp; }
+      if (m1 <= w) { stk[sp] = code | (base + c1); stkd[sp] = m1; ++sp; }
+      if (m0 <= w) {
+        lvl = lvl + 1;
+        j = base + c0;
+        continue;
+      }
+    }
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      if (stkd[sp] <= L.d[K - 1]) {
+        lvl = (int)(stk[sp] >> 28);
+        j = stk[sp] & 0x0fffffffu;
+        found = true;
+        break;
+      }
+    }
+    if (!found) break;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Camera rays, src/ray_marching.cu:70-79.
+
+struct Ray {
+  float ox, oy, oz;
+  float dx, dy, dz;
+  float t_near, t_far;
+};
+
+// pane = (float)W / (2 * tanf(0.5 * fov)), evaluated on the device as the
+// reference's render kernel does (src/ray_marching.cu:74).
+__device__ __forceinline__ float view_pane(int width, float fov) {
+  return __fdiv_rn((float)width, __fmul_rn(2.0f, tanf(__fmul_rn(0.5f, fov))));
+}
+
+// m: column-major cam-to-world (column c at m[4c..4c+3]).
+__device__ __forceinline__ Ray make_ray(const float* m, int width, int height, float pane, int x,
+                                        int y) {
+  Ray r;
+  float ux = __fdiv_rn(__fsub_rn(__fmul_rn(2.0f, (float)x), (float)width), 2.0f);
+  float uy = __fdiv_rn(__fsub_rn(__fmul_rn(2.0f, (float)y), (float)height), 2.0f);
+  float uz = -pane;
+  float v[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float a = __fmaf_rn(m[0 + i], ux, __fmul_rn(m[4 + i], uy));
+    float b = __fmaf_rn(m[8 + i], uz, __fmul_rn(m[12 + i], 0.0f));
+    v[i] = __fadd_rn(a, b);
+  }
+  float len2 = __fadd_rn(__fmaf_rn(v[0], v[0], __fmul_rn(v[1], v[1])),
+                         __fmaf_rn(v[2], v[2], __fmul_rn(v[3], v[3])));
+  float inv = __fdiv_rn(1.0f, __fsqrt_rn(len2));
+  r.dx = __fmul_rn(v[0], inv);
+  r.dy = __fmul_rn(v[1], inv);
+  r.dz = __fmul_rn(v[2], inv);
+  float cx = -m[8], cy = -m[9], cz = -m[10];
+  float dd = __fmaf_rn(cz, r.dz, __fmaf_rn(cx, r.dx, __fmul_rn(cy, r.dy)));
+  r.t_far = __fdiv_rn(ZFAR, dd);
+  r.t_near = __fdiv_rn(ZNEAR, dd);
+  r.ox = m[12];
+  r.oy = m[13];
+  r.oz = m[14];
+  return r;
+}
+
+// One distance-function evaluation (src/ray_marching.cu:260-292): exact
+// 10-NN of p, then min of sqrtf(d2) - radius visiting candidates in
+// (d2, index) order with a strict "<".  Returns the step and the sorted
+// position of the chosen point (-1 if the cloud is empty).
+__device__ __forceinline__ float distance_step(const IndexDev& ix, float px, float py, float pz,
+                                               int32_t* best_s, bool* ok) {
+  KList<KNN> L;
+  *ok = knn_search<KNN>(ix, px, py, pz, L);
+  float best = __int_as_float(0x7f800000);
+  int32_t bs = -1;
+#pragma unroll
+  for (int j = 0; j < KNN; ++j) {
+    if (L.s[j] >= 0) {
+      float v = __fsub_rn(__fsqrt_rn(L.d[j]), L.r[j]);
+      if (v < best) {
+        best = v;
+        bs = L.s[j];
+      }
+    }
+  }
+  *best_s = bs;
+  return best;
+}
+
+// Sphere trace of one ray (src/ray_marching.cu:202-228).  Returns the
+// sorted position of the hit (or -1) and writes depth and the number of
+// distance evaluations.  `t_stop` <= t_far is the culling bound: beyond it
+// no sphere can come within MIN_DIST of the ray (see the culling kernel).
+struct MarchResult {
+  int32_t s;
+  float depth;
+  int32_t steps;
+  bool ok;
+};
+
+__device__ __forceinline__ MarchResult march_ray(const IndexDev& ix, const Ray& r, float t_stop) {
+  MarchResult res;
+  res.s = -1;
+  res.depth = 0.0f;
+  res.steps = 0;
+  res.ok = true;
+  float t = r.t_near;
+  for (int i = 0; i < MAX_STEPS; ++i) {
+    if (t > t_stop) break;  // culled: the remaining steps cannot hit
+    float px = __fmaf_rn(r.dx, t, r.ox);
+    float py = __fmaf_rn(r.dy, t, r.oy);
+    float pz = __fmaf_rn(r.dz, t, r.oz);
+    int32_t s;
+    bool ok;
+    float step = distance_step(ix, px, py, pz, &s, &ok);
+    res.ok &= ok;
+    ++res.steps;
+    t = __fadd_rn(t, step);
+    if (step < MIN_DIST) {
+      res.s = s;
+      res.depth = t;
+      return res;
+    }
+    if (t > r.t_far) break;
+  }
+  return res;
+}
+
+}  // namespace rm

@@ -1,0 +1,73 @@
+// rm_radii.cu -- exact nearest-neighbour radii and the general kNN query.
+//
+// Replaces the reference's radii precompute (main.cu:107-113): FLANN
+// nearestKernel with k = 2 (kdtree_cuda_3d_index.cu:132-154, one thread per
+// query, result arrays in global memory), followed by a host loop doing 2N
+// synchronous device_reference copies for sqrt, and a separate clamp pass
+// (main.cu:144-149).  Here one kernel does search, sqrt, clamp and the
+// scatter back to cloud order.  Threads walk the points in index (Morton)
+// order, so the 32 queries of a warp are spatial neighbours and their tree
+// walks touch the same groups and leaves (L1/L2 hits).
+#include "rm_internal.h"
+
+namespace rm {
+
+__global__ void __launch_bounds__(128)
+k_radii(IndexDev ix, float max_radius, float* __restrict__ radii_out, int32_t* __restrict__ nn_out,
+        float* __restrict__ radii_clamped, unsigned long long* __restrict__ err) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ix.n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    float4 q = __ldg(ix.rec + s);
+    KList<2> L;
+    if (!knn_search<2>(ix, q.x, q.y, q.z, L)) atomicAdd(err, 1ull);
+    // sqrt of the second entry (main.cu:111); +inf when the cloud has one point
+    float r = __fsqrt_rn(L.d[1]);
+    int32_t i = __ldg(ix.perm + s);
+    if (radii_out) radii_out[i] = r;
+    if (nn_out) nn_out[i] = L.s[1] >= 0 ? __ldg(ix.perm + L.s[1]) : -1;
+    radii_clamped[i] = (max_radius > 0.0f && r > max_radius) ? max_radius : r;
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(128)
+k_knn(IndexDev ix, const float* __restrict__ q, int stride, int64_t m, int k,
+      int32_t* __restrict__ idx_out, float* __restrict__ d2_out, unsigned long long* __restrict__ err) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float* p = q + t * stride;
+    KList<K> L;
+    if (!knn_search<K>(ix, p[0], p[1], p[2], L)) atomicAdd(err, 1ull);
+    for (int j = 0; j < k; ++j) {
+      int32_t s = L.s[j];
+      idx_out[t * k + j] = s >= 0 ? __ldg(ix.perm + s) : -1;
+      d2_out[t * k + j] = L.d[j];
+    }
+  }
+}
+
+static int blocks_for(const Ctx& c, int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)c.sm_count * 64;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+void launch_radii(Ctx& c, float max_radius, float* radii_out, int32_t* nn_out) {
+  unsigned long long* err = c.scalars.ptr<unsigned long long>() + 8;
+  k_radii<<<blocks_for(c, c.n, 128), 128, 0, c.stream>>>(c.index(), max_radius, radii_out, nn_out,
+                                                         c.radii_clamped.ptr<float>(), err);
+}
+
+void launch_knn(Ctx& c, const float* q, int stride, int64_t m, int k, int32_t* idx, float* d2) {
+  unsigned long long* err = c.scalars.ptr<unsigned long long>() + 8;
+  int b = blocks_for(c, m, 128);
+  IndexDev ix = c.index();
+  if (k <= 2) k_knn<2><<<b, 128, 0, c.stream>>>(ix, q, stride, m, k, idx, d2, err);
+  else if (k <= 10) k_knn<10><<<b, 128, 0, c.stream>>>(ix, q, stride, m, k, idx, d2, err);
+  else if (k <= 16) k_knn<16><<<b, 128, 0, c.stream>>>(ix, q, stride, m, k, idx, d2, err);
+  else k_knn<32><<<b, 128, 0, c.stream>>>(ix, q, stride, m, k, idx, d2, err);
+}
+
+}  // namespace rm

@@ -1,0 +1,194 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Bit-exact for neighbour indices, squared distances, radii, hit indices and
+depths (the kernels and the oracle evaluate the same float32 operation
+sequence); colour equals the hit point's uint8 colour / 255.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from renderer_ray_marching_gb300 import Renderer, synthetic as syn, views_from_specs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene100k():
+    sc = syn.make_scene(100_000, n_boxes=12, seed=0)
+    ix = oracle.Index(sc.xyz)
+    return sc, ix
+
+
+def make_renderer(xyz, rgb=None, leaf=16, max_radius=0.1):
+    r = Renderer(leaf_size=leaf)
+    r.set_cloud(xyz, rgb)
+    r.build_index()
+    radii, nn = r.compute_radii(max_radius)
+    return r, radii, nn
+
+
+def oracle_view(r: Renderer, v):
+    pane = r.view_pane([v])[0]
+    return oracle.make_view(v.cam2world, v.width, v.height, float(pane))
+
+
+@pytest.mark.parametrize("n", [1, 5, 12, 1000, 30000])
+@pytest.mark.parametrize("k", [1, 2, 10, 16, 32])
+def test_knn_bit_exact(n, k):
+    rng = np.random.default_rng(n + 7 * k)
+    xyz = rng.normal(size=(n, 3)).astype(np.float32)
+    if n >= 12:
+        xyz[3:7] = xyz[1]  # duplicates
+    q = np.concatenate([xyz[: min(n, 200)], rng.normal(size=(300, 3)).astype(np.float32) * 2,
+                        rng.normal(size=(20, 3)).astype(np.float32) * 100])
+    r = Renderer()
+    r.set_cloud(xyz)
+    r.build_index()
+    gi, gd = r.knn(q, k)
+    oi, od = oracle.Index(xyz).knn(q, k)
+    assert np.array_equal(gi, oi)
+    assert np.array_equal(gd.view(np.int32), od.view(np.int32))
+
+
+def test_knn_empty_cloud_pads():
+    r = Renderer()
+    r.set_cloud(np.zeros((0, 3), np.float32))
+    r.build_index()
+    gi, gd = r.knn(np.zeros((4, 3), np.float32), 3)
+    assert np.all(gi == -1) and np.all(np.isinf(gd))
+
+
+@pytest.mark.parametrize("leaf", [8, 16, 32])
+def test_radii_bit_exact(scene100k, leaf):
+    sc, ix = scene100k
+    r, radii, nn = make_renderer(sc.xyz, sc.rgb, leaf=leaf)
+    orad, onn = ix.radii(0.0)
+    assert np.array_equal(radii.view(np.int32), orad.view(np.int32))
+    assert np.array_equal(nn, onn)
+
+
+def test_radii_golden_flann_fixture():
+    import os
+    g = os.path.join(os.path.dirname(__file__), "golden")
+    knn = np.load(os.path.join(g, "knn_flann.npz"))
+    gold = np.load(os.path.join(g, "radii_flann.npz"))
+    r, radii, nn = make_renderer(knn["xyz"])
+    assert np.array_equal(radii.view(np.int32), gold["radii"].view(np.int32))
+    assert np.array_equal(nn, gold["nn"])
+
+
+def test_radii_single_point_and_clamp():
+    r, radii, nn = make_renderer(np.array([[1, 2, 3]], np.float32), max_radius=0.05)
+    assert np.isinf(radii[0]) and nn[0] == -1
+
+
+def test_render_plain_matches_oracle(scene100k):
+    sc, ix = scene100k
+    r, radii, _ = make_renderer(sc.xyz, sc.rgb)
+    v = views_from_specs(syn.make_views(1, seed=1, boxes=sc.boxes))[0]
+    assert (v.width, v.height) == (1067, 690)
+    out = r.render(v, outputs=("rgbd", "hit", "depth", "steps"))
+    pix = np.random.default_rng(0).choice(v.pixels, 20000, replace=False).astype(np.int64)
+    oh, od, os_ = ix.render(np.minimum(radii, np.float32(0.1)), oracle_view(r, v), pix)
+    gh = out["hit"].reshape(-1)[pix]
+    gd = out["depth"].reshape(-1)[pix]
+    gs = out["steps"].reshape(-1)[pix]
+    assert np.array_equal(gh, oh)
+    assert np.array_equal(gd.view(np.int32), od.view(np.int32))
+    assert np.array_equal(gs, os_)
+    # colour = uint8 / 255 of the hit point, depth in .w; background zero
+    rgbd = out["rgbd"].reshape(-1, 4)
+    hits = out["hit"].reshape(-1)
+    m = hits >= 0
+    assert m.mean() > 0.5
+    col = (sc.rgb[hits[m]].astype(np.float32) / np.float32(255.0)).astype(np.float32)
+    assert np.array_equal(rgbd[m, :3], col)
+    assert np.array_equal(rgbd[m, 3], out["depth"].reshape(-1)[m])
+    assert np.all(rgbd[~m] == 0)
+
+
+def test_render_batch_equals_plain(scene100k):
+    sc, _ = scene100k
+    r, radii, _ = make_renderer(sc.xyz, sc.rgb)
+    specs = syn.make_views(6, seed=9, boxes=sc.boxes, resolutions=[(160, 120), (213, 138), (96, 54)])
+    views = views_from_specs(specs)
+    plain = [r.render(v, outputs=("rgbd", "hit", "depth", "steps")) for v in views]
+    for launch in [(8, 4, 1, 4), (8, 4, 2, 4), (4, 8, 4, 2), (16, 2, 2, 8)]:
+        r.set_launch(*launch)
+        batch = r.render_batch(views, outputs=("rgbd", "hit", "depth", "steps"), device=False)
+        for p, b in zip(plain, batch):
+            for key in ("hit", "steps"):
+                assert np.array_equal(p[key], b[key]), (launch, key)
+            assert np.array_equal(p["rgbd"].view(np.int32), b["rgbd"].view(np.int32)), launch
+    # a second replay of the cached graph gives the same answer
+    again = r.render_batch(views, outputs=("hit",), device=False)
+    for p, b in zip(plain, again):
+        assert np.array_equal(p["hit"], b["hit"])
+
+
+def test_render_independent_of_leaf_size(scene100k):
+    sc, _ = scene100k
+    v = views_from_specs(syn.make_views(1, seed=4, boxes=sc.boxes, resolutions=[(200, 150)]))[0]
+    outs = []
+    for leaf in (8, 16, 32):
+        r, _, _ = make_renderer(sc.xyz, sc.rgb, leaf=leaf)
+        outs.append(r.render(v))
+    for o in outs[1:]:
+        assert np.array_equal(o["hit"], outs[0]["hit"])
+        assert np.array_equal(o["depth"].view(np.int32), outs[0]["depth"].view(np.int32))
+
+
+@pytest.mark.parametrize("n", [0, 1, 5, 11])
+def test_render_tiny_clouds(n):
+    rng = np.random.default_rng(n)
+    xyz = (rng.random((n, 3)) * [8, 6, 3]).astype(np.float32)
+    r = Renderer()
+    r.set_cloud(xyz)
+    r.build_index()
+    radii, _ = r.compute_radii(0.5)
+    v = views_from_specs(syn.make_views(1, seed=2, resolutions=[(48, 32)]))[0]
+    out = r.render(v, outputs=("hit", "depth", "steps"))
+    if n == 0:
+        assert np.all(out["hit"] == -1)
+        return
+    ix = oracle.Index(xyz)
+    oh, od, os_ = ix.render(np.minimum(radii, np.float32(0.5)), oracle_view(r, v))
+    assert np.array_equal(out["hit"].reshape(-1), oh)
+    assert np.array_equal(out["depth"].reshape(-1).view(np.int32), od.view(np.int32))
+    assert np.array_equal(out["steps"].reshape(-1), os_)
+
+
+def test_cached_radii_path_equals_computed(scene100k):
+    sc, _ = scene100k
+    r, radii, _ = make_renderer(sc.xyz, sc.rgb)
+    v = views_from_specs(syn.make_views(1, seed=5, boxes=sc.boxes, resolutions=[(120, 90)]))[0]
+    a = r.render(v)
+    r2 = Renderer()
+    r2.set_cloud(sc.xyz, sc.rgb)
+    r2.set_radii(radii, 0.1)       # radii before the index (main.cu:122-149 order)
+    r2.build_index()
+    b = r2.render(v)
+    r3 = Renderer()
+    r3.set_cloud(sc.xyz, sc.rgb)
+    r3.build_index()
+    r3.set_radii(radii, 0.1)       # radii after the index
+    c = r3.render(v)
+    for o in (b, c):
+        assert np.array_equal(a["hit"], o["hit"])
+        assert np.array_equal(a["depth"].view(np.int32), o["depth"].view(np.int32))
+
+
+def test_errors_are_status_codes_not_exits():
+    from renderer_ray_marching_gb300._abi import RmError
+    r = Renderer()
+    v = views_from_specs(syn.make_views(1, seed=2, resolutions=[(8, 8)]))[0]
+    with pytest.raises(RmError, match="RM_ERR_STATE"):
+        r.render(v)
+    r.set_cloud(np.zeros((10, 3), np.float32))
+    with pytest.raises(RmError, match="RM_ERR_INVALID"):
+        r.set_radii(np.zeros(9, np.float32))
+    with pytest.raises(RmError, match="RM_ERR_INVALID"):
+        r.set_cloud(np.array([[0, np.nan, 0]], np.float32)) or r.build_index()
+    with pytest.raises(RmError, match="RM_ERR_INVALID"):
+        r.set_launch(8, 8, 1, 4)
