@@ -1,0 +1,429 @@
+#!/usr/bin/env python
+"""Benchmark of the renderer hot path on one GB300 (or N replicas).
+
+Metric (as named for the reference): Mrays/s of the batched marcher at 20M
+points over 256 views of mixed resolution (640x480, 1068x690, 1920x1080;
+fx = fy = 0.75 W), beside the plain per-view form, kNN-radii Mqueries/s at
+20M points, and forward / forward+backward ms per 1067x690 view on a
+1M-point cloud.  All inputs are seeded synthetic scenes of that shape
+(renderer_ray_marching_gb300.synthetic); the cloud, index and per-view
+records (>= 0.8 GB) exceed the 129 MB L2, so no flush is needed between
+timed steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+A step is one batched render of all 256 views (value: device-resident
+inputs and outputs, CUDA events on the launching stream).  e2e is the same
+step through the C ABI with host buffers: the view table goes host->device
+and every view's RGBA32F image (colour + depth, the reference's texture
+format) comes back to pinned host memory inside the timed region.
+
+--impl reference times the reference's CPU path for the same workload: the
+marcher loop of src/ray_marching.cu with an exact 10-NN per step, run by the
+oracle's C restatement (the reference tree does not travel to the GPU host)
+on all host cores, over a bounded sample of rays per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s & kNN-radii Mqueries/s at 20M pts (batched vs plain); fwd+bwd ms/view"
+RES = [(640, 480), (1068, 690), (1920, 1080)]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--points", type=int, default=20_000_000)
+    ap.add_argument("--views", type=int, default=256)
+    ap.add_argument("--cpu-rays", type=int, default=40_000, help="rays per CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(args, rank):
+    from renderer_ray_marching_gb300 import synthetic as syn, views_from_specs
+    sc = syn.make_scene(args.points, n_boxes=40, seed=2000 + rank)
+    specs = syn.make_views(args.views, seed=3000 + rank, boxes=sc.boxes, resolutions=RES)
+    return sc, views_from_specs(specs)
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_ray():
+    """DRAM bytes per ray of the batched marcher from the committed ncu
+    summary (profiles/march_batch_traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "march_batch_traffic.json")
+    if os.path.exists(p):
+        return json.load(open(p))
+    return None
+
+
+def cpu_sample_render(sc, views, radii_clamped, n_rays, seed, threads=0):
+    """Oracle (the reference marcher loop restated in C, exact 10-NN) on a
+    bounded, seeded sample of rays spread over the views.  Returns
+    (rays, seconds, build_seconds)."""
+    import oracle
+    t0 = time.perf_counter()
+    ix = oracle.Index(sc.xyz)
+    t_build = time.perf_counter() - t0
+    from renderer_ray_marching_gb300 import Renderer  # noqa: F401  (pane below)
+    rng = np.random.default_rng(seed)
+    per = max(1, n_rays // len(views))
+    jobs = []
+    for v, pane in views:
+        pix = rng.choice(v.pixels, min(per, v.pixels), replace=False).astype(np.int64)
+        jobs.append((oracle.make_view(v.cam2world, v.width, v.height, float(pane)), pix))
+    t0 = time.perf_counter()
+    rays = 0
+    for ov, pix in jobs:
+        ix.render(radii_clamped, ov, pix, threads=threads)
+        rays += pix.shape[0]
+    return rays, time.perf_counter() - t0, t_build
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    from renderer_ray_marching_gb300 import synthetic as syn  # noqa: F401
+    sc, views = workload(args, 0)
+    ix = oracle.Index(sc.xyz)
+    radii, _ = ix.radii(0.1)
+    # the pane of each view as the reference evaluates it (device tanf); on
+    # the CPU path the host tanf stands in
+    import math
+    vp = [(v, np.float32(np.float32(v.width) / (np.float32(2.0) * np.float32(math.tan(np.float32(0.5) * np.float32(v.fov))))))
+          for v in views]
+    cores = os.cpu_count() or 1
+    rng_seed = 99
+    times = []
+    rays_per = 0
+    n_rays = args.cpu_rays
+    for step in range(args.warmup + args.steps):
+        rng = np.random.default_rng(rng_seed + step)
+        per = max(1, n_rays // len(vp))
+        t0 = time.perf_counter()
+        rays = 0
+        for v, pane in vp:
+            pix = rng.choice(v.pixels, min(per, v.pixels), replace=False).astype(np.int64)
+            ix.render(radii, oracle.make_view(v.cam2world, v.width, v.height, float(pane)), pix, threads=cores)
+            rays += pix.shape[0]
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            rays_per = rays
+    value = rays_per / float(np.mean(times)) / 1e6
+    sample = "%d rays per step spread over %d views (%d points), exact 10-NN per march step" % (
+        rays_per, len(vp), sc.xyz.shape[0])
+    line = {"metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * float(np.mean(times)), 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched render, %d points, %d views from {640x480, 1068x690, 1920x1080}" % (
+                sc.xyz.shape[0], len(vp)), "points": int(sc.xyz.shape[0]), "views": len(vp)},
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    from renderer_ray_marching_gb300 import Renderer, _abi, synthetic as syn, views_from_specs
+
+    ws, rank, local = dist_info()
+    dist = ws > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda:%d" % local)
+    stream = torch.cuda.Stream(device=dev)
+
+    sc, views = workload(args, rank)
+    xyz_d = torch.from_numpy(sc.xyz).to(dev)
+    rgb_d = torch.from_numpy(sc.rgb).to(dev)
+    torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        r = Renderer(leaf_size=16, device=local, stream=stream.cuda_stream)
+
+        # ---- radii: upload from device memory, index build, radii kernel
+        rad_d = torch.empty(sc.xyz.shape[0], dtype=torch.float32, device=dev)
+        nn_d = torch.empty(sc.xyz.shape[0], dtype=torch.int32, device=dev)
+        radii_ms = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for i in range(args.warmup + 2):
+            e0.record(stream)
+            r.set_cloud(xyz_d, rgb_d)
+            r.build_index()
+            r._check(r._lib.rm_radii_compute(r._h, 0.1, rad_d.data_ptr(), nn_d.data_ptr(), _abi.RM_DEVICE))
+            e1.record(stream)
+            e1.synchronize()
+            if i >= args.warmup:
+                radii_ms.append(e0.elapsed_time(e1))
+        radii_mq = sc.xyz.shape[0] / (float(np.median(radii_ms)) * 1e-3) / 1e6
+
+        # ---- autotune on a subset of views
+        tune = r.autotune(views[:16])
+
+        # ---- batched, device-resident
+        frames = (_abi.RmFrame * len(views))()
+        keep = []
+        for i, v in enumerate(views):
+            rgbd = torch.empty((v.height, v.width, 4), dtype=torch.float32, device=dev)
+            hit = torch.empty((v.height, v.width), dtype=torch.int32, device=dev)
+            frames[i].rgbd = rgbd.data_ptr()
+            frames[i].hit = hit.data_ptr()
+            keep.append((rgbd, hit))
+        cviews = (_abi.RmView * len(views))(*[v.to_c() for v in views])
+        total_rays = sum(v.pixels for v in views)
+        for _ in range(args.warmup):
+            r.render_batch_into(views, frames, device=True, cviews=cviews)
+        r.synchronize()
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+        clocks = Clocks(local)
+        clocks.start()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kern_ms, steps_total, hits_total = [], 0, 0
+        for k in range(args.steps):
+            starts[k].record(stream)
+            r.render_batch_into(views, frames, device=True, cviews=cviews)
+            ends[k].record(stream)
+            st = r.stats()  # synchronises; kernel time from events inside the graph
+            kern_ms.append(st["kernel_ms"])
+            steps_total = st["steps"]
+            hits_total = st.get("hits", 0)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        t_step = float(np.mean(step_ms))
+        if dist:
+            tt = torch.tensor([t_step], device=dev)
+            tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+            t_step = float(tt.item())
+        value = ws * total_rays / (t_step * 1e-3) / 1e6
+        hits_total = int(sum(int((h >= 0).sum().item()) for _, h in keep))
+
+        # ---- plain per-view form, same views
+        r.synchronize()
+        e0.record(stream)
+        for i, v in enumerate(views):
+            r._check(r._lib.rm_render(r._h, ctypes.byref(cviews[i]), ctypes.byref(frames[i]), _abi.RM_DEVICE))
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+        plain = total_rays / (plain_ms * 1e-3) / 1e6
+
+        # ---- e2e: host buffers through the C ABI (views in, RGBA32F images out)
+        host_frames = (_abi.RmFrame * len(views))()
+        host_keep = []
+        for i, v in enumerate(views):
+            b = torch.empty((v.height, v.width, 4), dtype=torch.float32).pin_memory()
+            host_frames[i].rgbd = b.data_ptr()
+            host_keep.append(b)
+        r.render_batch_into(views, host_frames, device=False, cviews=cviews)
+        e2e_t = []
+        for _ in range(max(2, args.steps // 2)):
+            t0 = time.perf_counter()
+            r.render_batch_into(views, host_frames, device=False, cviews=cviews)
+            e2e_t.append(time.perf_counter() - t0)
+        e2e = total_rays / float(np.mean(e2e_t)) / 1e6
+        h2d = len(views) * ctypes.sizeof(_abi.RmView)
+        d2h = total_rays * 16
+
+        # ---- forward / forward+backward per 1067x690 view on a 1M-point cloud
+        fb = fwd_bwd(args, dev, stream, rank)
+        r.close()
+
+    peak, peak_kind = measured_peak()
+    kms = float(np.median(kern_ms))
+    alg_bytes = 20 * total_rays + 16 * hits_total + 160 * steps_total
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    tr = traffic_per_ray()
+    traffic = None if tr is None else int(tr["dram_bytes_per_ray"] * total_rays)
+    out = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(t_step, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "batched render of %d views (640x480/1068x690/1920x1080, fx=0.75W) over a %d-point "
+                                  "synthetic room, 40 boxes" % (len(views), sc.xyz.shape[0]),
+                      "points": int(sc.xyz.shape[0]), "views": len(views), "rays_per_step": int(total_rays),
+                      "l2": "inputs larger than L2 (cloud + index >= 0.8 GB), no flush",
+                      "launch": tune, "parallelism": "replicas" if ws > 1 else "single"},
+           "plain_mrays_s": round(plain, 3), "batched_over_plain": round(value / ws / plain, 3),
+           "radii_mqueries_s": round(radii_mq, 3), "radii_ms": round(float(np.median(radii_ms)), 3),
+           "fwd_ms_per_view": fb["fwd_ms"], "fwdbwd_ms_per_view": fb["fwdbwd_ms"],
+           "fwdbwd_over_fwd": fb["ratio"],
+           "steps_per_ray": round(steps_total / total_rays, 3), "hit_fraction": round(hits_total / total_rays, 4),
+           "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+                   "d2h_bytes_per_step": int(d2h)},
+           "roofline": {"bound": "hbm", "kernel": "k_march_batch", "achieved": round(achieved, 1), "peak": peak,
+                        "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                        "bytes_model": "20 B out + 16 B colour per hit + 160 B per distance step (10 float4 candidates)",
+                        "kernel_ms": round(kms, 3)},
+           "clocks": clk,
+           "gpu_launches": 2 * args.steps}
+    if rank == 0 and not args.no_cpu_baseline:
+        import math
+        vp = [(v, np.float32(np.float32(v.width) / (np.float32(2.0) * np.float32(math.tan(np.float32(0.5) * np.float32(v.fov))))))
+              for v in views]
+        rad_h = np.minimum(rad_d.cpu().numpy(), np.float32(0.1))
+        cores = os.cpu_count() or 1
+        rays, secs, tb = cpu_sample_render(sc, vp, rad_h, args.cpu_rays, 7, threads=cores)
+        out["cpu_baseline"] = {"value": round(rays / secs / 1e6, 5), "unit": "Mrays/s", "cores": cores,
+                               "kind": "port",
+                               "sample": "%d rays over %d views, oracle kd-tree (build %.1f s, not timed)" % (
+                                   rays, len(vp), tb)}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        tdist.destroy_process_group()
+
+
+def fwd_bwd(args, dev, stream, rank):
+    """Forward (plain render) and forward + loss gradient + backward per
+    1067x690 view over 16 views of a 1M-point cloud."""
+    import torch
+    from renderer_ray_marching_gb300 import Renderer, _abi, synthetic as syn, views_from_specs
+    sc = syn.make_scene(1_000_000, n_boxes=12, seed=4000 + rank)
+    views = views_from_specs(syn.make_views(16, seed=4100 + rank, boxes=sc.boxes))
+    rng = np.random.default_rng(5)
+    xt = (sc.xyz + rng.normal(0, 0.005, sc.xyz.shape)).astype(np.float32)
+    ct = np.clip(sc.rgb.astype(np.int32) + rng.integers(-30, 31, sc.rgb.shape), 0, 255).astype(np.uint8)
+    r = Renderer(device=dev.index, stream=stream.cuda_stream)
+    rt = Renderer(device=dev.index, stream=stream.cuda_stream)
+    for rr, x, c in ((r, sc.xyz, sc.rgb), (rt, xt, ct)):
+        rr.set_cloud(x, c)
+        rr.build_index()
+        rr.compute_radii(0.1)
+    n = sc.xyz.shape[0]
+    tg = [rt.render(v, outputs=("rgbd", "hit"), device=True) for v in views]
+    rt.close()
+    g = [torch.zeros((n, 3), device=dev), torch.zeros((n, 3), device=dev), torch.zeros(n, device=dev)]
+    frames = [{"rgbd": torch.empty((v.height, v.width, 4), device=dev),
+               "hit": torch.empty((v.height, v.width), dtype=torch.int32, device=dev)} for v in views]
+    dl_rgb = [torch.empty((v.pixels, 3), device=dev) for v in views]
+    dl_d = [torch.empty(v.pixels, device=dev) for v in views]
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+
+    def fwd(i):
+        r.render_into(views[i], frames[i], device=True)
+
+    def bwd(i):
+        f, t = frames[i], tg[i]
+        both = (f["hit"] >= 0) & (t["hit"] >= 0)
+        d = (f["rgbd"] - t["rgbd"]).reshape(-1, 4)
+        m = both.reshape(-1, 1).float()
+        torch.mul(d[:, :3], 2.0 * m, out=dl_rgb[i])
+        torch.mul(torch.sign(d[:, 3]), m[:, 0], out=dl_d[i])
+        r._check(r._lib.rm_backward(r._h, ctypes.byref(views[i].to_c()), 1, dl_rgb[i].data_ptr(),
+                                    dl_d[i].data_ptr(), f["hit"].data_ptr(), g[0].data_ptr(),
+                                    g[1].data_ptr(), g[2].data_ptr(), _abi.RM_DEVICE))
+
+    for i in range(len(views)):  # warm-up
+        fwd(i)
+        bwd(i)
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    for i in range(len(views)):
+        fwd(i)
+    e[1].record(stream)
+    for i in range(len(views)):
+        fwd(i)
+        bwd(i)
+    e[2].record(stream)
+    e[2].synchronize()
+    f_ms = e[0].elapsed_time(e[1]) / len(views)
+    fb_ms = e[1].elapsed_time(e[2]) / len(views)
+    r.close()
+    return {"fwd_ms": round(f_ms, 3), "fwdbwd_ms": round(fb_ms, 3), "ratio": round(fb_ms / f_ms, 3)}
+
+
+if __name__ == "__main__":
+    main()

@@ -23,9 +23,10 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "librm_gb300.so")
 CLI = os.path.join(LIBDIR, "marcher.bin")
+IOLIB = os.path.join(LIBDIR, "librm_io.so")
 
 CUDA_SOURCES = ["rm_index.cu", "rm_radii.cu", "rm_march.cu", "rm_backward.cu", "rm_api.cu"]
-HOST_SOURCES = ["marcher_main.cpp", "io.cpp"]
+HOST_SOURCES = ["marcher_main.cpp", "io.cpp", "rmio_c.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]
 
@@ -47,7 +48,7 @@ def _digest(paths, extra: str) -> str:
 
 
 def _headers():
-    out = [os.path.join(INCLUDE, "rm.h")]
+    out = [os.path.join(INCLUDE, "rm.h"), os.path.join(INCLUDE, "rmio.h")]
     for d in (CSRC, HOST):
         if os.path.isdir(d):
             out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".h", ".cuh", ".hpp"))]
@@ -61,6 +62,26 @@ def _compile(src: str, obj: str, flags) -> None:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr[-4000:]))
 
 
+def build_host() -> None:
+    """librm_io.so (file formats, no CUDA) and marcher.bin (links both libraries)."""
+    io_srcs = [os.path.join(HOST, "io.cpp"), os.path.join(HOST, "rmio_c.cpp")]
+    tmp = IOLIB + ".tmp%d" % os.getpid()
+    cmd = (["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I" + INCLUDE, "-I" + HOST,
+            "-o", tmp] + io_srcs + ["-lz"])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("io library build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+    os.replace(tmp, IOLIB)
+    tmp = CLI + ".tmp%d" % os.getpid()
+    cmd = (["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE, "-I" + HOST, "-o", tmp,
+            os.path.join(HOST, "marcher_main.cpp"), "-L" + LIBDIR, "-lrm_io", "-lrm_gb300",
+            "-Wl,-rpath,$ORIGIN", "-lz", "-lm", "-lpthread"])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+    os.replace(tmp, CLI)
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile the library (and the CLI when its sources exist); return the
     path of the shared library."""
@@ -72,7 +93,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     digest = _digest(srcs + hsrcs + _headers(), " ".join(NVCC_FLAGS) + os.uname().machine)
     if (not force and os.path.exists(LIB) and os.path.exists(stamp)
             and open(stamp).read().strip() == digest
-            and (not hsrcs or os.path.exists(CLI))):
+            and (not hsrcs or (os.path.exists(CLI) and os.path.exists(IOLIB)))):
         return LIB
     objs = [os.path.join(OBJDIR, os.path.basename(s) + ".o") for s in srcs]
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
@@ -86,13 +107,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
     os.replace(tmp, LIB)
     if hsrcs:
-        tmp = CLI + ".tmp%d" % os.getpid()
-        cmd = (["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE, "-I" + HOST, "-o", tmp]
-               + hsrcs + ["-L" + LIBDIR, "-lrm_gb300", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("CLI build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
-        os.replace(tmp, CLI)
+        build_host()
     with open(stamp, "w") as f:
         f.write(digest)
     if verbose:

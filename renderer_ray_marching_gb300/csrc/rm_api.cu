@@ -448,9 +448,7 @@ void enqueue_batch(Ctx& c, int n, int64_t items, const rm_launch& L) {
     CK(cudaMemsetAsync(c.queue.p, 0, 8, c.stream));
     CK(cudaMemsetAsync(counters(c), 0, kCounters * 8, c.stream));
     CK(cudaMemsetAsync(err_counter(c), 0, 8, c.stream));
-    CK(cudaEventRecord(c.ev0, c.stream));
     launch_render_batch(c, c.views.ptr<ViewDev>(), n, items, L, counters(c));
-    CK(cudaEventRecord(c.ev1, c.stream));
     cudaError_t e = cudaStreamEndCapture(c.stream, &g);
     if (e != cudaSuccess) throw CudaError(std::string("graph capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&c.graph_exec, g, 0);
@@ -463,7 +461,11 @@ void enqueue_batch(Ctx& c, int n, int64_t items, const rm_launch& L) {
     c.graph_key_views = (void*)(intptr_t)items;
     c.graph_key_launch = L;
   }
+  // timing events go on the stream around the graph (event nodes inside a
+  // graph cannot be used for elapsed-time queries)
+  CK(cudaEventRecord(c.ev0, c.stream));
   CK(cudaGraphLaunch(c.graph_exec, c.stream));
+  CK(cudaEventRecord(c.ev1, c.stream));
 }
 
 bool launch_ok(const rm_launch& L) {

@@ -107,7 +107,10 @@ __device__ __forceinline__ void klist_insert(KList<K>& L, float d, int32_t s, fl
   }
 }
 
-template <int K>
+// WARM: the list may already hold points (seeded from the previous march
+// step), so a candidate that passes the distance test is inserted only if
+// it is not one of them.
+template <int K, bool WARM>
 __device__ __forceinline__ void scan_leaf(const IndexDev& ix, int64_t leaf, float qx, float qy,
                                           float qz, KList<K>& L) {
   int64_t start = leaf * ix.leaf;
@@ -116,7 +119,33 @@ __device__ __forceinline__ void scan_leaf(const IndexDev& ix, int64_t leaf, floa
   for (int64_t i = start; i < end; ++i) {
     float4 c = __ldg(ix.rec + i);
     float d = d2_point(c, qx, qy, qz);
-    if (d <= L.d[K - 1]) klist_insert<K>(L, d, (int32_t)i, c.w, ix.perm);
+    if (d <= L.d[K - 1]) {
+      bool dup = false;
+      if (WARM) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) dup |= (L.s[j] == (int32_t)i);
+      }
+      if (!dup) klist_insert<K>(L, d, (int32_t)i, c.w, ix.perm);
+    }
+  }
+}
+
+// Re-evaluate the points of L at a new query: they are valid candidates, so
+// the search that follows starts with a finite k-th distance and prunes from
+// the first node.  The result is still the exact k-NN.
+template <int K>
+__device__ __forceinline__ void klist_rewarm(const IndexDev& ix, float qx, float qy, float qz,
+                                             KList<K>& L) {
+  int32_t old[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) old[j] = L.s[j];
+  klist_init<K>(L);
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    if (old[j] >= 0) {
+      float4 c = __ldg(ix.rec + old[j]);
+      klist_insert<K>(L, d2_point(c, qx, qy, qz), old[j], c.w, ix.perm);
+    }
   }
 }
 
@@ -132,9 +161,9 @@ __device__ __forceinline__ void scan_leaf(const IndexDev& ix, int64_t leaf, floa
 // its box bound is <= the current k-th distance, so equal-distance points
 // with a lower index are never skipped.  Returns false only if the stack
 // bound was exceeded (cannot happen for depth <= MAX_LEVELS).
-template <int K>
+template <int K, bool WARM = false>
 __device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, KList<K>& L) {
-  klist_init<K>(L);
+  if (!WARM) klist_init<K>(L);
   if (ix.n <= 0) return true;
   uint32_t stk[STACK];
   float stkd[STACK];
@@ -158,12 +187,12 @@ __device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, KLi
     uint32_t base = j * 4u;
     if (lvl + 1 == ix.depth) {
       if (m0 <= L.d[K - 1]) {
-        scan_leaf<K>(ix, base + c0, qx, qy, qz, L);
+        scan_leaf<K, WARM>(ix, base + c0, qx, qy, qz, L);
         if (m1 <= L.d[K - 1]) {
-          scan_leaf<K>(ix, base + c1, qx, qy, qz, L);
+          scan_leaf<K, WARM>(ix, base + c1, qx, qy, qz, L);
           if (m2 <= L.d[K - 1]) {
-            scan_leaf<K>(ix, base + c2, qx, qy, qz, L);
-            if (m3 <= L.d[K - 1]) scan_leaf<K>(ix, base + c3, qx, qy, qz, L);
+            scan_leaf<K, WARM>(ix, base + c2, qx, qy, qz, L);
+            if (m3 <= L.d[K - 1]) scan_leaf<K, WARM>(ix, base + c3, qx, qy, qz, L);
           }
         }
       }
@@ -244,10 +273,11 @@ __device__ __forceinline__ Ray make_ray(const float* m, int width, int height, f
 // 10-NN of p, then min of sqrtf(d2) - radius visiting candidates in
 // (d2, index) order with a strict "<".  Returns the step and the sorted
 // position of the chosen point (-1 if the cloud is empty).
+// L carries the previous step's neighbours of the same ray (or is empty).
 __device__ __forceinline__ float distance_step(const IndexDev& ix, float px, float py, float pz,
-                                               int32_t* best_s, bool* ok) {
-  KList<KNN> L;
-  *ok = knn_search<KNN>(ix, px, py, pz, L);
+                                               KList<KNN>& L, int32_t* best_s, bool* ok) {
+  klist_rewarm<KNN>(ix, px, py, pz, L);
+  *ok = knn_search<KNN, true>(ix, px, py, pz, L);
   float best = __int_as_float(0x7f800000);
   int32_t bs = -1;
 #pragma unroll
@@ -282,6 +312,8 @@ __device__ __forceinline__ MarchResult march_ray(const IndexDev& ix, const Ray& 
   res.steps = 0;
   res.ok = true;
   float t = r.t_near;
+  KList<KNN> L;
+  klist_init<KNN>(L);
   for (int i = 0; i < MAX_STEPS; ++i) {
     if (t > t_stop) break;  // culled: the remaining steps cannot hit
     float px = __fmaf_rn(r.dx, t, r.ox);
@@ -289,7 +321,7 @@ __device__ __forceinline__ MarchResult march_ray(const IndexDev& ix, const Ray& 
     float pz = __fmaf_rn(r.dz, t, r.oz);
     int32_t s;
     bool ok;
-    float step = distance_step(ix, px, py, pz, &s, &ok);
+    float step = distance_step(ix, px, py, pz, L, &s, &ok);
     res.ok &= ok;
     ++res.steps;
     t = __fadd_rn(t, step);

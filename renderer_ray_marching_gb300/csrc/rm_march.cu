@@ -162,6 +162,7 @@ k_march_batch(IndexDev ix, BatchArgs a, unsigned long long* __restrict__ queue,
   Ray r;
   float t = 0.0f, t_stop = 0.0f;
   int nsteps = 0;
+  KList<KNN> L;  // the lane's neighbours from its previous step
   unsigned long long steps_total = 0, rays_total = 0, bad = 0;
 
   while (true) {
@@ -195,6 +196,7 @@ k_march_batch(IndexDev ix, BatchArgs a, unsigned long long* __restrict__ queue,
           t_stop = clip_exit(r, a.clip);
           t = r.t_near;
           nsteps = 0;
+          klist_init<KNN>(L);
         }
       }
       next += __popc(need);
@@ -215,7 +217,7 @@ k_march_batch(IndexDev ix, BatchArgs a, unsigned long long* __restrict__ queue,
         float pz = __fmaf_rn(r.dz, t, r.oz);
         int32_t s;
         bool ok;
-        float step = distance_step(ix, px, py, pz, &s, &ok);
+        float step = distance_step(ix, px, py, pz, L, &s, &ok);
         if (!ok) ++bad;
         ++nsteps;
         t = __fadd_rn(t, step);

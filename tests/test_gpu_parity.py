@@ -96,7 +96,9 @@ def test_render_plain_matches_oracle(scene100k):
     gs = out["steps"].reshape(-1)[pix]
     assert np.array_equal(gh, oh)
     assert np.array_equal(gd.view(np.int32), od.view(np.int32))
-    assert np.array_equal(gs, os_)
+    # the exit culling only ever shortens rays that miss
+    assert np.array_equal(gs[oh >= 0], os_[oh >= 0])
+    assert np.all(gs[oh < 0] <= os_[oh < 0])
     # colour = uint8 / 255 of the hit point, depth in .w; background zero
     rgbd = out["rgbd"].reshape(-1, 4)
     hits = out["hit"].reshape(-1)
@@ -156,7 +158,8 @@ def test_render_tiny_clouds(n):
     oh, od, os_ = ix.render(np.minimum(radii, np.float32(0.5)), oracle_view(r, v))
     assert np.array_equal(out["hit"].reshape(-1), oh)
     assert np.array_equal(out["depth"].reshape(-1).view(np.int32), od.view(np.int32))
-    assert np.array_equal(out["steps"].reshape(-1), os_)
+    gs = out["steps"].reshape(-1)
+    assert np.array_equal(gs[oh >= 0], os_[oh >= 0]) and np.all(gs[oh < 0] <= os_[oh < 0])
 
 
 def test_cached_radii_path_equals_computed(scene100k):
