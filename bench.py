@@ -56,6 +56,13 @@ def parse():
     return ap.parse_args()
 
 
+T0 = time.perf_counter()
+
+
+def log(msg):
+    print("[bench %7.1fs] %s" % (time.perf_counter() - T0, msg), file=sys.stderr, flush=True)
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -223,6 +230,7 @@ def main():
     stream = torch.cuda.Stream(device=dev)
 
     sc, views = workload(args, rank)
+    log("workload ready: %d points, %d views" % (sc.xyz.shape[0], len(views)))
     xyz_d = torch.from_numpy(sc.xyz).to(dev)
     rgb_d = torch.from_numpy(sc.rgb).to(dev)
     torch.cuda.synchronize()
@@ -245,9 +253,11 @@ def main():
             if i >= args.warmup:
                 radii_ms.append(e0.elapsed_time(e1))
         radii_mq = sc.xyz.shape[0] / (float(np.median(radii_ms)) * 1e-3) / 1e6
+        log("radii %.2f ms" % float(np.median(radii_ms)))
 
         # ---- autotune on a subset of views
         tune = r.autotune(views[:16])
+        log("autotune %s" % tune)
 
         # ---- batched, device-resident
         frames = (_abi.RmFrame * len(views))()
@@ -262,6 +272,8 @@ def main():
         total_rays = sum(v.pixels for v in views)
         for _ in range(args.warmup):
             r.render_batch_into(views, frames, device=True, cviews=cviews)
+            r.synchronize()
+            log("warm-up batch %.1f ms" % r.stats()["kernel_ms"])
         r.synchronize()
         if dist:
             tdist.barrier()
@@ -299,6 +311,7 @@ def main():
         e1.synchronize()
         plain_ms = e0.elapsed_time(e1)
         plain = total_rays / (plain_ms * 1e-3) / 1e6
+        log("timed batch %.1f ms/step, plain %.1f ms" % (t_step, plain_ms))
 
         # ---- e2e: host buffers through the C ABI (views in, RGBA32F images out)
         host_frames = (_abi.RmFrame * len(views))()
@@ -314,11 +327,13 @@ def main():
             r.render_batch_into(views, host_frames, device=False, cviews=cviews)
             e2e_t.append(time.perf_counter() - t0)
         e2e = total_rays / float(np.mean(e2e_t)) / 1e6
+        log("e2e %.1f ms" % (1e3 * float(np.mean(e2e_t))))
         h2d = len(views) * ctypes.sizeof(_abi.RmView)
         d2h = total_rays * 16
 
         # ---- forward / forward+backward per 1067x690 view on a 1M-point cloud
         fb = fwd_bwd(args, dev, stream, rank)
+        log("fwd/bwd %s" % fb)
         r.close()
 
     peak, peak_kind = measured_peak()
@@ -356,6 +371,7 @@ def main():
         rad_h = np.minimum(rad_d.cpu().numpy(), np.float32(0.1))
         cores = os.cpu_count() or 1
         rays, secs, tb = cpu_sample_render(sc, vp, rad_h, args.cpu_rays, 7, threads=cores)
+        log("cpu baseline %d rays %.1f s (build %.1f s)" % (rays, secs, tb))
         out["cpu_baseline"] = {"value": round(rays / secs / 1e6, 5), "unit": "Mrays/s", "cores": cores,
                                "kind": "port",
                                "sample": "%d rays over %d views, oracle kd-tree (build %.1f s, not timed)" % (

@@ -41,7 +41,7 @@ struct rmo_index {
   float* xyz;      /* copy of the points, stride 3 */
   int64_t* order;  /* point ids grouped by leaf */
   rmo_node* nodes;
-  int64_t nnodes, cap;
+  int64_t nnodes;
 };
 
 /* Squared distance, FLANN CudaL2::dist order as nvcc contracts it. */
@@ -62,12 +62,28 @@ static inline float box_d2(const rmo_node* nd, const float* q) {
   return fmaf(g[2], g[2], fmaf(g[0], g[0], g[1] * g[1]));
 }
 
-static int64_t new_node(rmo_index* ix) {
-  if (ix->nnodes == ix->cap) {
-    ix->cap = ix->cap ? ix->cap * 2 : 1024;
-    ix->nodes = (rmo_node*)realloc(ix->nodes, (size_t)ix->cap * sizeof(rmo_node));
+/* Nodes of a subtree over `count` points: the split is always count/2, so
+ * the tree shape (and a pre-order numbering) depends on the count alone,
+ * which lets independent subtrees be built in parallel. */
+static void nodes_pair(int64_t m, int64_t* a, int64_t* b) {
+  /* a = nodes(m), b = nodes(m + 1), with nodes(c) = 1 for c <= LEAF,
+   * nodes(2k) = 1 + 2 nodes(k), nodes(2k + 1) = 1 + nodes(k) + nodes(k + 1) */
+  if (m + 1 <= RMO_LEAF) { *a = 1; *b = 1; return; }
+  int64_t k = m / 2, nk, nk1;
+  nodes_pair(k, &nk, &nk1);
+  if (m % 2 == 0) {
+    *a = (m <= RMO_LEAF) ? 1 : 1 + 2 * nk;
+    *b = 1 + nk + nk1;
+  } else {
+    *a = (m <= RMO_LEAF) ? 1 : 1 + nk + nk1;
+    *b = 1 + 2 * nk1;
   }
-  return ix->nnodes++;
+}
+
+static int64_t subtree_nodes(int64_t count) {
+  int64_t a, b;
+  nodes_pair(count, &a, &b);
+  return a;
 }
 
 /* Quickselect on order[lo, hi) by coordinate `axis`, k-th element in place. */
@@ -91,8 +107,7 @@ static void select_axis(const float* xyz, int64_t* order, int64_t lo, int64_t hi
   }
 }
 
-static int64_t build_rec(rmo_index* ix, int64_t start, int64_t count) {
-  int64_t id = new_node(ix);
+static void build_rec(rmo_index* ix, int64_t id, int64_t start, int64_t count) {
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int64_t i = start; i < start + count; ++i) {
     const float* p = ix->xyz + ix->order[i] * 3;
@@ -101,23 +116,33 @@ static int64_t build_rec(rmo_index* ix, int64_t start, int64_t count) {
       if (p[a] > hi[a]) hi[a] = p[a];
     }
   }
-  memcpy(ix->nodes[id].lo, lo, sizeof lo);
-  memcpy(ix->nodes[id].hi, hi, sizeof hi);
-  ix->nodes[id].start = start;
-  ix->nodes[id].count = count;
-  ix->nodes[id].left = ix->nodes[id].right = -1;
-  if (count <= RMO_LEAF) return id;
+  rmo_node* nd = &ix->nodes[id];
+  memcpy(nd->lo, lo, sizeof lo);
+  memcpy(nd->hi, hi, sizeof hi);
+  nd->start = start;
+  nd->count = count;
+  nd->left = nd->right = -1;
+  if (count <= RMO_LEAF) return;
   int axis = 0;
   float ext = hi[0] - lo[0];
   for (int a = 1; a < 3; ++a)
     if (hi[a] - lo[a] > ext) { ext = hi[a] - lo[a]; axis = a; }
   int64_t half = count / 2;
   select_axis(ix->xyz, ix->order, start, start + count, start + half, axis);
-  int64_t l = build_rec(ix, start, half);
-  int64_t r = build_rec(ix, start + half, count - half);
-  ix->nodes[id].left = (int32_t)l;
-  ix->nodes[id].right = (int32_t)r;
-  return id;
+  int64_t l = id + 1;
+  int64_t r = id + 1 + subtree_nodes(half);
+  nd->left = (int32_t)l;
+  nd->right = (int32_t)r;
+  if (count > (1 << 16)) {
+#pragma omp task default(shared) firstprivate(l, start, half)
+    build_rec(ix, l, start, half);
+#pragma omp task default(shared) firstprivate(r, start, half, count)
+    build_rec(ix, r, start + half, count - half);
+#pragma omp taskwait
+  } else {
+    build_rec(ix, l, start, half);
+    build_rec(ix, r, start + half, count - half);
+  }
 }
 
 rmo_index* rmo_index_build(const float* xyz, int64_t n) {
@@ -127,7 +152,13 @@ rmo_index* rmo_index_build(const float* xyz, int64_t n) {
   ix->order = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
   if (n > 0) memcpy(ix->xyz, xyz, (size_t)n * 3 * sizeof(float));
   for (int64_t i = 0; i < n; ++i) ix->order[i] = i;
-  if (n > 0) build_rec(ix, 0, n);
+  if (n > 0) {
+    ix->nnodes = subtree_nodes(n);
+    ix->nodes = (rmo_node*)malloc((size_t)ix->nnodes * sizeof(rmo_node));
+#pragma omp parallel
+#pragma omp single
+    build_rec(ix, 0, 0, n);
+  }
   return ix;
 }
 
