@@ -53,6 +53,12 @@ def parse():
     ap.add_argument("--views", type=int, default=256)
     ap.add_argument("--cpu-rays", type=int, default=40_000, help="rays per CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # switches for short profiling runs (never used for a reported number)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-fwdbwd", action="store_true")
+    ap.add_argument("--resolution", default=None, help="WxH for every view instead of the mixed set")
     return ap.parse_args()
 
 
@@ -73,7 +79,11 @@ def dist_info():
 def workload(args, rank):
     from renderer_ray_marching_gb300 import synthetic as syn, views_from_specs
     sc = syn.make_scene(args.points, n_boxes=40, seed=2000 + rank)
-    specs = syn.make_views(args.views, seed=3000 + rank, boxes=sc.boxes, resolutions=RES)
+    res = RES
+    if getattr(args, "resolution", None):
+        w, h = (int(x) for x in args.resolution.lower().split("x"))
+        res = [(w, h)]
+    specs = syn.make_views(args.views, seed=3000 + rank, boxes=sc.boxes, resolutions=res)
     return sc, views_from_specs(specs)
 
 
@@ -241,23 +251,28 @@ def main():
         # ---- radii: upload from device memory, index build, radii kernel
         rad_d = torch.empty(sc.xyz.shape[0], dtype=torch.float32, device=dev)
         nn_d = torch.empty(sc.xyz.shape[0], dtype=torch.int32, device=dev)
-        radii_ms = []
+        radii_ms, build_ms, query_ms = [], [], []
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        em = torch.cuda.Event(enable_timing=True)
         for i in range(args.warmup + 2):
             e0.record(stream)
             r.set_cloud(xyz_d, rgb_d)
             r.build_index()
+            em.record(stream)
             r._check(r._lib.rm_radii_compute(r._h, 0.1, rad_d.data_ptr(), nn_d.data_ptr(), _abi.RM_DEVICE))
             e1.record(stream)
             e1.synchronize()
             if i >= args.warmup:
                 radii_ms.append(e0.elapsed_time(e1))
+                build_ms.append(e0.elapsed_time(em))
+                query_ms.append(em.elapsed_time(e1))
         radii_mq = sc.xyz.shape[0] / (float(np.median(radii_ms)) * 1e-3) / 1e6
-        log("radii %.2f ms" % float(np.median(radii_ms)))
+        log("radii %.2f ms (upload+build %.2f, query %.2f)" % (float(np.median(radii_ms)), float(np.median(build_ms)),
+                                                             float(np.median(query_ms))))
 
         # ---- autotune on a subset of views
-        tune = r.autotune(views[:16])
-        log("autotune %s" % tune)
+        tune = r.get_launch() if args.no_autotune else r.autotune(views[:16])
+        log("launch %s" % tune)
 
         # ---- batched, device-resident
         frames = (_abi.RmFrame * len(views))()
@@ -273,7 +288,7 @@ def main():
         for _ in range(args.warmup):
             r.render_batch_into(views, frames, device=True, cviews=cviews)
             r.synchronize()
-            log("warm-up batch %.1f ms" % r.stats()["kernel_ms"])
+            log("warm-up batch %s" % r.stats())
         r.synchronize()
         if dist:
             tdist.barrier()
@@ -303,37 +318,43 @@ def main():
         hits_total = int(sum(int((h >= 0).sum().item()) for _, h in keep))
 
         # ---- plain per-view form, same views
-        r.synchronize()
-        e0.record(stream)
-        for i, v in enumerate(views):
-            r._check(r._lib.rm_render(r._h, ctypes.byref(cviews[i]), ctypes.byref(frames[i]), _abi.RM_DEVICE))
-        e1.record(stream)
-        e1.synchronize()
-        plain_ms = e0.elapsed_time(e1)
-        plain = total_rays / (plain_ms * 1e-3) / 1e6
-        log("timed batch %.1f ms/step, plain %.1f ms" % (t_step, plain_ms))
+        plain, plain_ms = None, None
+        if not args.skip_plain:
+            r.synchronize()
+            e0.record(stream)
+            for i, v in enumerate(views):
+                r._check(r._lib.rm_render(r._h, ctypes.byref(cviews[i]), ctypes.byref(frames[i]), _abi.RM_DEVICE))
+            e1.record(stream)
+            e1.synchronize()
+            plain_ms = e0.elapsed_time(e1)
+            plain = total_rays / (plain_ms * 1e-3) / 1e6
+        log("timed batch %.1f ms/step, plain %s ms" % (t_step, plain_ms))
 
         # ---- e2e: host buffers through the C ABI (views in, RGBA32F images out)
-        host_frames = (_abi.RmFrame * len(views))()
-        host_keep = []
-        for i, v in enumerate(views):
-            b = torch.empty((v.height, v.width, 4), dtype=torch.float32).pin_memory()
-            host_frames[i].rgbd = b.data_ptr()
-            host_keep.append(b)
-        r.render_batch_into(views, host_frames, device=False, cviews=cviews)
-        e2e_t = []
-        for _ in range(max(2, args.steps // 2)):
-            t0 = time.perf_counter()
+        e2e, h2d, d2h = None, 0, 0
+        if not args.skip_e2e:
+            host_frames = (_abi.RmFrame * len(views))()
+            host_keep = []
+            for i, v in enumerate(views):
+                b = torch.empty((v.height, v.width, 4), dtype=torch.float32).pin_memory()
+                host_frames[i].rgbd = b.data_ptr()
+                host_keep.append(b)
             r.render_batch_into(views, host_frames, device=False, cviews=cviews)
-            e2e_t.append(time.perf_counter() - t0)
-        e2e = total_rays / float(np.mean(e2e_t)) / 1e6
-        log("e2e %.1f ms" % (1e3 * float(np.mean(e2e_t))))
-        h2d = len(views) * ctypes.sizeof(_abi.RmView)
-        d2h = total_rays * 16
+            e2e_t = []
+            for _ in range(max(2, args.steps // 2)):
+                t0 = time.perf_counter()
+                r.render_batch_into(views, host_frames, device=False, cviews=cviews)
+                e2e_t.append(time.perf_counter() - t0)
+            e2e = total_rays / float(np.mean(e2e_t)) / 1e6
+            h2d = len(views) * ctypes.sizeof(_abi.RmView)
+            d2h = total_rays * 16
+            log("e2e %.1f ms" % (1e3 * float(np.mean(e2e_t))))
 
         # ---- forward / forward+backward per 1067x690 view on a 1M-point cloud
-        fb = fwd_bwd(args, dev, stream, rank)
-        log("fwd/bwd %s" % fb)
+        fb = {"fwd_ms": None, "fwdbwd_ms": None, "ratio": None}
+        if not args.skip_fwdbwd:
+            fb = fwd_bwd(args, dev, stream, rank)
+            log("fwd/bwd %s" % fb)
         r.close()
 
     peak, peak_kind = measured_peak()
@@ -350,12 +371,14 @@ def main():
                       "points": int(sc.xyz.shape[0]), "views": len(views), "rays_per_step": int(total_rays),
                       "l2": "inputs larger than L2 (cloud + index >= 0.8 GB), no flush",
                       "launch": tune, "parallelism": "replicas" if ws > 1 else "single"},
-           "plain_mrays_s": round(plain, 3), "batched_over_plain": round(value / ws / plain, 3),
+           "plain_mrays_s": None if plain is None else round(plain, 3),
+           "batched_over_plain": None if plain is None else round(value / ws / plain, 3),
            "radii_mqueries_s": round(radii_mq, 3), "radii_ms": round(float(np.median(radii_ms)), 3),
+           "radii_build_ms": round(float(np.median(build_ms)), 3), "radii_query_ms": round(float(np.median(query_ms)), 3),
            "fwd_ms_per_view": fb["fwd_ms"], "fwdbwd_ms_per_view": fb["fwdbwd_ms"],
            "fwdbwd_over_fwd": fb["ratio"],
            "steps_per_ray": round(steps_total / total_rays, 3), "hit_fraction": round(hits_total / total_rays, 4),
-           "e2e": {"value": round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
+           "e2e": {"value": None if e2e is None else round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
            "roofline": {"bound": "hbm", "kernel": "k_march_batch", "achieved": round(achieved, 1), "peak": peak,
                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,

@@ -87,16 +87,21 @@ typedef struct {
 typedef struct {
   int64_t rays;          /* rays marched */
   int64_t steps;         /* total distance-function evaluations */
-  int64_t tiles_culled;  /* ray tiles that the culling pass retired */
-  float kernel_ms;       /* device time of the marching kernel(s) */
+  int64_t hits;          /* rays that hit a sphere */
+  int64_t coop_steps;    /* steps answered by a warp's shared gather */
+  int64_t solo_steps;    /* steps answered by a per-ray tree search */
+  int64_t gather_overflows; /* warp steps whose gather exceeded its capacity */
+  float kernel_ms;       /* device time of the last render launch (graph for the batch) */
 } rm_stats;
 
-/* Batched-form launch parameters (picked by rm_autotune or set by hand). */
+/* Marcher launch parameters (picked by rm_autotune or set by hand). */
 typedef struct {
   int32_t tile_w;        /* warp tile width in pixels (tile_w * tile_h == 32) */
   int32_t tile_h;
-  int32_t rays_per_lane; /* rays a warp claims per lane when it takes a tile */
-  int32_t ctas_per_sm;   /* persistent CTAs per SM */
+  int32_t rays_per_lane; /* tiles per work item; a lane whose ray ends takes the item's next pixel */
+  int32_t ctas_per_sm;   /* persistent CTAs per SM (batched form) */
+  float coop_radius;     /* metres: a ray whose current 10th-neighbour distance is at most this joins
+                            its warp's shared candidate gather (0: every step searches alone) */
 } rm_launch;
 
 void rm_config_default(rm_config* cfg);

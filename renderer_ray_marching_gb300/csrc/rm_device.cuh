@@ -107,45 +107,126 @@ __device__ __forceinline__ void klist_insert(KList<K>& L, float d, int32_t s, fl
   }
 }
 
-// WARM: the list may already hold points (seeded from the previous march
-// step), so a candidate that passes the distance test is inserted only if
-// it is not one of them.
-template <int K, bool WARM>
+template <int K>
+__device__ __forceinline__ float klist_worst(const KList<K>& L) {
+  return L.d[K - 1];
+}
+
+// The marcher's 10 nearest, kept as an unsorted set with its worst entry
+// (largest (d2, cloud index)) tracked: an insertion replaces the worst slot,
+// and re-seeding at the next step's position re-measures the ten points
+// without sorting.  Insertions skip points already present, so the set can
+// start from the previous step's points (they are valid candidates: the
+// search then prunes with a finite bound from the first node and stays exact).
+struct KSet {
+  float d[KNN];
+  int32_t s[KNN];   // sorted position, -1 = empty
+  float r[KNN];
+  float wd;         // worst entry: d2, position, slot
+  int32_t ws;
+  int wi;
+
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      d[j] = __int_as_float(0x7f800000);
+      s[j] = -1;
+      r[j] = 0.0f;
+    }
+    wd = __int_as_float(0x7f800000);
+    ws = -1;
+    wi = 0;
+  }
+
+  __device__ __forceinline__ void recompute_worst(const int32_t* __restrict__ perm) {
+    wd = d[0];
+    ws = s[0];
+    wi = 0;
+#pragma unroll
+    for (int j = 1; j < KNN; ++j) {
+      bool later = d[j] > wd;
+      if (!later && d[j] == wd && ws >= 0) later = s[j] < 0 || __ldg(perm + s[j]) > __ldg(perm + ws);
+      if (later) {
+        wd = d[j];
+        ws = s[j];
+        wi = j;
+      }
+    }
+  }
+
+  // Candidate (dd, ss) with dd <= wd.
+  __device__ __forceinline__ void consider(float dd, int32_t ss, float rr,
+                                           const int32_t* __restrict__ perm) {
+    if (dd == wd && ws >= 0 && !(__ldg(perm + ss) < __ldg(perm + ws))) return;
+    bool dup = false;
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) dup |= (s[j] == ss);
+    if (dup) return;
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      if (j == wi) {
+        d[j] = dd;
+        s[j] = ss;
+        r[j] = rr;
+      }
+    }
+    recompute_worst(perm);
+  }
+
+  __device__ __forceinline__ void rewarm(const IndexDev& ix, float qx, float qy, float qz) {
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      if (s[j] >= 0) d[j] = d2_point(__ldg(ix.rec + s[j]), qx, qy, qz);
+    }
+    recompute_worst(ix.perm);
+  }
+
+  // src/ray_marching.cu:280-290: min of sqrtf(d2) - r visiting candidates
+  // in ascending (d2, index) order with a strict "<" -- equivalently the
+  // minimum value, ties going to the smaller (d2, index).
+  __device__ __forceinline__ float step_value(const int32_t* __restrict__ perm, int32_t* best_s) const {
+    float best = __int_as_float(0x7f800000), bd = best;
+    int32_t bs = -1;
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      if (s[j] >= 0) {
+        float v = __fsub_rn(__fsqrt_rn(d[j]), r[j]);
+        bool take = v < best;
+        if (!take && v == best)
+          take = d[j] < bd || (d[j] == bd && __ldg(perm + s[j]) < __ldg(perm + bs));
+        if (take) {
+          best = v;
+          bd = d[j];
+          bs = s[j];
+        }
+      }
+    }
+    *best_s = bs;
+    return best;
+  }
+};
+
+__device__ __forceinline__ float list_worst(const KSet& L) { return L.wd; }
+template <int K>
+__device__ __forceinline__ float list_worst(const KList<K>& L) { return L.d[K - 1]; }
+__device__ __forceinline__ void list_consider(KSet& L, float d, int32_t s, float r, const int32_t* perm) {
+  L.consider(d, s, r, perm);
+}
+template <int K>
+__device__ __forceinline__ void list_consider(KList<K>& L, float d, int32_t s, float r, const int32_t* perm) {
+  klist_insert<K>(L, d, s, r, perm);
+}
+
+template <class List>
 __device__ __forceinline__ void scan_leaf(const IndexDev& ix, int64_t leaf, float qx, float qy,
-                                          float qz, KList<K>& L) {
+                                          float qz, List& L) {
   int64_t start = leaf * ix.leaf;
   int64_t end = start + ix.leaf;
   if (end > ix.n) end = ix.n;
   for (int64_t i = start; i < end; ++i) {
     float4 c = __ldg(ix.rec + i);
     float d = d2_point(c, qx, qy, qz);
-    if (d <= L.d[K - 1]) {
-      bool dup = false;
-      if (WARM) {
-#pragma unroll
-        for (int j = 0; j < K; ++j) dup |= (L.s[j] == (int32_t)i);
-      }
-      if (!dup) klist_insert<K>(L, d, (int32_t)i, c.w, ix.perm);
-    }
-  }
-}
-
-// Re-evaluate the points of L at a new query: they are valid candidates, so
-// the search that follows starts with a finite k-th distance and prunes from
-// the first node.  The result is still the exact k-NN.
-template <int K>
-__device__ __forceinline__ void klist_rewarm(const IndexDev& ix, float qx, float qy, float qz,
-                                             KList<K>& L) {
-  int32_t old[K];
-#pragma unroll
-  for (int j = 0; j < K; ++j) old[j] = L.s[j];
-  klist_init<K>(L);
-#pragma unroll
-  for (int j = 0; j < K; ++j) {
-    if (old[j] >= 0) {
-      float4 c = __ldg(ix.rec + old[j]);
-      klist_insert<K>(L, d2_point(c, qx, qy, qz), old[j], c.w, ix.perm);
-    }
+    if (d <= list_worst(L)) list_consider(L, d, (int32_t)i, c.w, ix.perm);
   }
 }
 
@@ -161,9 +242,9 @@ __device__ __forceinline__ void klist_rewarm(const IndexDev& ix, float qx, float
 // its box bound is <= the current k-th distance, so equal-distance points
 // with a lower index are never skipped.  Returns false only if the stack
 // bound was exceeded (cannot happen for depth <= MAX_LEVELS).
-template <int K, bool WARM = false>
-__device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, KList<K>& L) {
-  if (!WARM) klist_init<K>(L);
+// The caller initialises (or seeds) L.
+template <class List>
+__device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, List& L) {
   if (ix.n <= 0) return true;
   uint32_t stk[STACK];
   float stkd[STACK];
@@ -186,18 +267,18 @@ __device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, KLi
     RM_CSWAP(m1, c1, m2, c2);
     uint32_t base = j * 4u;
     if (lvl + 1 == ix.depth) {
-      if (m0 <= L.d[K - 1]) {
-        scan_leaf<K, WARM>(ix, base + c0, qx, qy, qz, L);
-        if (m1 <= L.d[K - 1]) {
-          scan_leaf<K, WARM>(ix, base + c1, qx, qy, qz, L);
-          if (m2 <= L.d[K - 1]) {
-            scan_leaf<K, WARM>(ix, base + c2, qx, qy, qz, L);
-            if (m3 <= L.d[K - 1]) scan_leaf<K, WARM>(ix, base + c3, qx, qy, qz, L);
+      if (m0 <= list_worst(L)) {
+        scan_leaf(ix, base + c0, qx, qy, qz, L);
+        if (m1 <= list_worst(L)) {
+          scan_leaf(ix, base + c1, qx, qy, qz, L);
+          if (m2 <= list_worst(L)) {
+            scan_leaf(ix, base + c2, qx, qy, qz, L);
+            if (m3 <= list_worst(L)) scan_leaf(ix, base + c3, qx, qy, qz, L);
           }
         }
       }
     } else {
-      float w = L.d[K - 1];
+      float w = list_worst(L);
       if (sp + 3 > STACK) return false;
       uint32_t code = (uint32_t)(lvl + 1) << 28;
       if (m3 <= w) { stk[sp] = code | (base + c3); stkd[sp] = m3; ++sp; }
@@ -212,7 +293,7 @@ __device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, KLi
     bool found = false;
     while (sp > 0) {
       --sp;
-      if (stkd[sp] <= L.d[K - 1]) {
+      if (stkd[sp] <= list_worst(L)) {
         lvl = (int)(stk[sp] >> 28);
         j = stk[sp] & 0x0fffffffu;
         found = true;
@@ -267,72 +348,6 @@ __device__ __forceinline__ Ray make_ray(const float* m, int width, int height, f
   r.oy = m[13];
   r.oz = m[14];
   return r;
-}
-
-// One distance-function evaluation (src/ray_marching.cu:260-292): exact
-// 10-NN of p, then min of sqrtf(d2) - radius visiting candidates in
-// (d2, index) order with a strict "<".  Returns the step and the sorted
-// position of the chosen point (-1 if the cloud is empty).
-// L carries the previous step's neighbours of the same ray (or is empty).
-__device__ __forceinline__ float distance_step(const IndexDev& ix, float px, float py, float pz,
-                                               KList<KNN>& L, int32_t* best_s, bool* ok) {
-  klist_rewarm<KNN>(ix, px, py, pz, L);
-  *ok = knn_search<KNN, true>(ix, px, py, pz, L);
-  float best = __int_as_float(0x7f800000);
-  int32_t bs = -1;
-#pragma unroll
-  for (int j = 0; j < KNN; ++j) {
-    if (L.s[j] >= 0) {
-      float v = __fsub_rn(__fsqrt_rn(L.d[j]), L.r[j]);
-      if (v < best) {
-        best = v;
-        bs = L.s[j];
-      }
-    }
-  }
-  *best_s = bs;
-  return best;
-}
-
-// Sphere trace of one ray (src/ray_marching.cu:202-228).  Returns the
-// sorted position of the hit (or -1) and writes depth and the number of
-// distance evaluations.  `t_stop` <= t_far is the culling bound: beyond it
-// no sphere can come within MIN_DIST of the ray (see the culling kernel).
-struct MarchResult {
-  int32_t s;
-  float depth;
-  int32_t steps;
-  bool ok;
-};
-
-__device__ __forceinline__ MarchResult march_ray(const IndexDev& ix, const Ray& r, float t_stop) {
-  MarchResult res;
-  res.s = -1;
-  res.depth = 0.0f;
-  res.steps = 0;
-  res.ok = true;
-  float t = r.t_near;
-  KList<KNN> L;
-  klist_init<KNN>(L);
-  for (int i = 0; i < MAX_STEPS; ++i) {
-    if (t > t_stop) break;  // culled: the remaining steps cannot hit
-    float px = __fmaf_rn(r.dx, t, r.ox);
-    float py = __fmaf_rn(r.dy, t, r.oy);
-    float pz = __fmaf_rn(r.dz, t, r.oz);
-    int32_t s;
-    bool ok;
-    float step = distance_step(ix, px, py, pz, L, &s, &ok);
-    res.ok &= ok;
-    ++res.steps;
-    t = __fadd_rn(t, step);
-    if (step < MIN_DIST) {
-      res.s = s;
-      res.depth = t;
-      return res;
-    }
-    if (t > r.t_far) break;
-  }
-  return res;
 }
 
 }  // namespace rm

@@ -19,7 +19,8 @@ k_radii(IndexDev ix, float max_radius, float* __restrict__ radii_out, int32_t* _
        s += (int64_t)gridDim.x * blockDim.x) {
     float4 q = __ldg(ix.rec + s);
     KList<2> L;
-    if (!knn_search<2>(ix, q.x, q.y, q.z, L)) atomicAdd(err, 1ull);
+    klist_init<2>(L);
+    if (!knn_search(ix, q.x, q.y, q.z, L)) atomicAdd(err, 1ull);
     // sqrt of the second entry (main.cu:111); +inf when the cloud has one point
     float r = __fsqrt_rn(L.d[1]);
     int32_t i = __ldg(ix.perm + s);
@@ -37,7 +38,8 @@ k_knn(IndexDev ix, const float* __restrict__ q, int stride, int64_t m, int k,
        t += (int64_t)gridDim.x * blockDim.x) {
     const float* p = q + t * stride;
     KList<K> L;
-    if (!knn_search<K>(ix, p[0], p[1], p[2], L)) atomicAdd(err, 1ull);
+    klist_init<K>(L);
+    if (!knn_search(ix, p[0], p[1], p[2], L)) atomicAdd(err, 1ull);
     for (int j = 0; j < k; ++j) {
       int32_t s = L.s[j];
       idx_out[t * k + j] = s >= 0 ? __ldg(ix.perm + s) : -1;
