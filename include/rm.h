@@ -88,9 +88,9 @@ typedef struct {
   int64_t rays;          /* rays marched */
   int64_t steps;         /* total distance-function evaluations */
   int64_t hits;          /* rays that hit a sphere */
-  int64_t coop_steps;    /* steps answered by a warp's shared gather */
-  int64_t solo_steps;    /* steps answered by a per-ray tree search */
-  int64_t gather_overflows; /* warp steps whose gather exceeded its capacity */
+  int64_t packet_steps;  /* steps answered by a warp packet traversal */
+  int64_t solo_steps;    /* steps answered by a per-ray tree walk */
+  int64_t packet_leaves; /* leaves scanned by packet traversals */
   float kernel_ms;       /* device time of the last render launch (graph for the batch) */
 } rm_stats;
 
@@ -100,8 +100,8 @@ typedef struct {
   int32_t tile_h;
   int32_t rays_per_lane; /* tiles per work item; a lane whose ray ends takes the item's next pixel */
   int32_t ctas_per_sm;   /* persistent CTAs per SM (batched form) */
-  float coop_radius;     /* metres: a ray whose current 10th-neighbour distance is at most this joins
-                            its warp's shared candidate gather (0: every step searches alone) */
+  int32_t search;        /* 1: the warp walks the index once for all its rays (packet
+                            traversal, default); 0: every ray walks it alone */
 } rm_launch;
 
 void rm_config_default(rm_config* cfg);

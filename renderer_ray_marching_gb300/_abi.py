@@ -45,14 +45,14 @@ class RmFrame(ctypes.Structure):
 
 class RmStats(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_int64), ("steps", ctypes.c_int64), ("hits", ctypes.c_int64),
-                ("coop_steps", ctypes.c_int64), ("solo_steps", ctypes.c_int64),
-                ("gather_overflows", ctypes.c_int64), ("kernel_ms", ctypes.c_float)]
+                ("packet_steps", ctypes.c_int64), ("solo_steps", ctypes.c_int64),
+                ("packet_leaves", ctypes.c_int64), ("kernel_ms", ctypes.c_float)]
 
 
 class RmLaunch(ctypes.Structure):
     _fields_ = [("tile_w", ctypes.c_int32), ("tile_h", ctypes.c_int32),
                 ("rays_per_lane", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("coop_radius", ctypes.c_float)]
+                ("search", ctypes.c_int32)]
 
 
 class RmError(RuntimeError):

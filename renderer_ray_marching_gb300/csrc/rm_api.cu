@@ -439,7 +439,7 @@ void enqueue_batch(Ctx& c, int n, int64_t items, const rm_launch& L) {
                 c.graph_key_launch.tile_w == L.tile_w && c.graph_key_launch.tile_h == L.tile_h &&
                 c.graph_key_launch.rays_per_lane == L.rays_per_lane &&
                 c.graph_key_launch.ctas_per_sm == L.ctas_per_sm &&
-                c.graph_key_launch.coop_radius == L.coop_radius;
+                c.graph_key_launch.search == L.search;
   if (!key_ok) {
     c.drop_graph();
     cudaGraph_t g;
@@ -472,7 +472,7 @@ void enqueue_batch(Ctx& c, int n, int64_t items, const rm_launch& L) {
 bool launch_ok(const rm_launch& L) {
   return L.tile_w > 0 && L.tile_h > 0 && L.tile_w * L.tile_h == 32 && L.rays_per_lane >= 1 &&
          L.rays_per_lane <= 16 && L.ctas_per_sm >= 1 && L.ctas_per_sm <= 16 &&
-         std::isfinite(L.coop_radius) && L.coop_radius >= 0.0f && L.coop_radius <= 100.0f;
+         (L.search == 0 || L.search == 1);
 }
 
 }  // namespace
@@ -540,9 +540,8 @@ rm_status rm_render_batch(rm_ctx* ctx, const rm_view* views, int32_t n, const rm
 
 rm_status rm_set_launch(rm_ctx* ctx, const rm_launch* launch) {
   return guarded(ctx, [&](Ctx& c) -> rm_status {
-    if (!launch || !launch_ok(*launch)) return fail(c, RM_ERR_INVALID, "rm_set_launch: tile_w*tile_h must be 32, 1<=rays_per_lane<=16, 1<=ctas_per_sm<=16, 0<=coop_radius<=100");
+    if (!launch || !launch_ok(*launch)) return fail(c, RM_ERR_INVALID, "rm_set_launch: tile_w*tile_h must be 32, 1<=rays_per_lane<=16, 1<=ctas_per_sm<=16, search 0 or 1");
     c.launch = *launch;
-    c.coop_radius = launch->coop_radius;
     c.drop_graph();
     return RM_OK;
   });
@@ -570,9 +569,9 @@ rm_status rm_get_stats(rm_ctx* ctx, rm_stats* stats) {
     c.stats.steps = (int64_t)h[0];
     c.stats.rays = (int64_t)h[1];
     c.stats.hits = (int64_t)h[2];
-    c.stats.coop_steps = (int64_t)h[4];
+    c.stats.packet_steps = (int64_t)h[4];
     c.stats.solo_steps = (int64_t)h[5];
-    c.stats.gather_overflows = (int64_t)h[6];
+    c.stats.packet_leaves = (int64_t)h[6];
     c.stats.kernel_ms = ms;
     *stats = c.stats;
     return RM_OK;
@@ -661,7 +660,6 @@ rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* c
     }
     auto time_once = [&](const rm_launch& L) -> float {
       c.launch = L;
-      c.coop_radius = L.coop_radius;
       float best = 1e30f;
       for (int rep = 0; rep < 2; ++rep) {
         rm_status s = rm_render_batch(ctx, views, n, fr.data(), RM_DEVICE);
@@ -679,14 +677,14 @@ rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* c
     float best_t = 1e30f;
     for (auto& sh : shapes)
       for (int rpl : rpls) {
-        rm_launch L{sh[0], sh[1], rpl, 4, best_l.coop_radius};
+        rm_launch L{sh[0], sh[1], rpl, 4, best_l.search};
         float t = time_once(L);
         if (t < best_t) { best_t = t; best_l = L; }
       }
-    for (float cr : {0.0f, 0.015f, 0.03f, 0.06f}) {
-      if (cr == best_l.coop_radius) continue;
+    for (int mode : {0, 1}) {
+      if (mode == best_l.search) continue;
       rm_launch L = best_l;
-      L.coop_radius = cr;
+      L.search = mode;
       float t = time_once(L);
       if (t < best_t) { best_t = t; best_l = L; }
     }
@@ -717,7 +715,6 @@ rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* c
     CK(cudaStreamSynchronize(c.stream));
     scratch.release();
     c.launch = best_l;
-    c.coop_radius = best_l.coop_radius;
     c.drop_graph();
     if (chosen) *chosen = best_l;
     if (leaf_size) *leaf_size = best_leaf;

@@ -104,8 +104,7 @@ struct Ctx {
   DevBuf frame_bufs;     // device outputs for host-side frames
   DevBuf queue;          // work-queue counters
 
-  rm_launch launch{8, 4, 1, 4, 0.03f};
-  float coop_radius = 0.03f;
+  rm_launch launch{8, 4, 1, 4, 1};
   rm_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -114,7 +113,7 @@ struct Ctx {
   std::vector<ViewDev> graph_views;
   void* graph_key_views = nullptr;
   int graph_key_n = -1;
-  rm_launch graph_key_launch{0, 0, 0, 0, 0.0f};
+  rm_launch graph_key_launch{0, 0, 0, 0, 0};
   void* pinned_views = nullptr;
   size_t pinned_views_cap = 0;
 

@@ -5,23 +5,25 @@
 // Work unit: one warp marches the rays of a screen tile (tile_w x tile_h
 // pixels, 32 rays; with rays_per_lane > 1 an item is rays_per_lane such
 // tiles stacked vertically and a lane whose ray ends takes the item's next
-// pixel).  Each distance step is an exact 10-NN of the step position:
+// pixel).  Each distance step is an exact 10-NN of every lane's step
+// position, found by a warp packet traversal:
 //
 //   1. seed: every lane re-measures its previous step's 10 points at the new
-//      position (valid candidates, so its k-th distance is finite at once);
-//   2. cooperative gather: lanes whose seeded ball (radius = sqrt of the
-//      seeded 10th distance) is small form a group; the warp takes the box Q
-//      holding all their balls and walks the tree once, 32 nodes per round,
-//      collecting every leaf whose box meets Q;
-//   3. staged scan: the warp copies those leaves' records into shared memory
-//      with coalesced loads and every lane of the group tests every staged
-//      point (shared-memory broadcast reads).  Every point inside a lane's
-//      ball lies in Q, hence in a collected leaf, so the lane's 10-NN is
-//      exact;
-//   4. lanes outside the group (first step, empty space), or all lanes when
-//      the gather exceeds its capacity, run the per-lane tree search.
-// Then the step value min(sqrtf(d2) - r) and the reference's termination
-// tests (MIN_DIST hit, far plane, MAX_STEPS).
+//      position (valid candidates, so its 10th distance is finite at once);
+//   2. the warp walks the tree once, as a unit: a node is expanded when its
+//      box lies within the current 10th distance of ANY active lane (one
+//      __ballot_sync per child), children are visited nearest-first for the
+//      leading lane, and a stack of pending boxes lives in shared memory so
+//      every pop is re-tested against the (shrinking) bounds of all lanes;
+//   3. a leaf's records are read once for the whole warp (broadcast loads)
+//      and every lane updates its own exact set, so all lanes' bounds tighten
+//      while the walk goes on.
+// Neighbouring rays need nearly the same leaves (at surfaces, and in open
+// space where the 10 nearest of every lane cluster around the same foot
+// point), so the warp pays for the union of their searches once instead of
+// serialising 32 divergent walks.  Search mode 0 keeps one independent walk
+// per lane.  Then the step value min(sqrtf(d2) - r) and the reference's
+// termination tests (MIN_DIST hit, far plane, MAX_STEPS).
 //
 // Plain form (rm_render): one warp per 8x4 tile, four warps per CTA.
 // Batched form (rm_render_batch): a persistent kernel whose warps pull items
@@ -68,22 +70,19 @@ __device__ __forceinline__ float clip_exit(const Ray& r, const ClipBox& e) {
   return tmax + fabsf(tmax) * 1e-5f + 1e-3f;
 }
 
-// Per-warp shared memory of the cooperative step.
+// Per-warp shared memory of the packet traversal: the stack of pending
+// nodes with their boxes (re-tested when popped).
 constexpr int WARPS_PER_CTA = 4;
-constexpr int FRONTIER_CAP = 128;   // nodes per tree level
-constexpr int LEAF_CAP = 128;       // leaves per gather
-constexpr int STAGE_CAP = 256;      // staged records per scan round
+constexpr int PSTACK = 3 * MAX_LEVELS + 4;
 
 struct WarpSmem {
-  uint32_t front[2][FRONTIER_CAP];
-  uint32_t leaves[LEAF_CAP];
-  float4 rec[STAGE_CAP];
-  int32_t pos[STAGE_CAP];
+  uint32_t code[PSTACK];
+  float box[PSTACK][6];
 };
 
 struct MarchParams {
   ClipBox clip;
-  float coop_r2;  // lanes whose seeded 10th distance (squared) is at most this join the gather
+  int search;  // 1: warp packet traversal, 0: one walk per lane
 };
 
 // View as seen by the marcher.
@@ -98,110 +97,130 @@ struct ViewArgs {
 };
 
 // counters: [0] steps, [1] rays, [2] hits, [3] search errors,
-//           [4] gathered lane-steps, [5] per-lane lane-steps, [6] gather overflows
+//           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets
 struct LaneCounters {
-  unsigned long long steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, overflow = 0;
+  unsigned long long steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0;
 };
 
-__device__ __forceinline__ float warp_min(float v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, off));
-  return v;
-}
-__device__ __forceinline__ float warp_max(float v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, off));
-  return v;
-}
+#define RM_CSWAP_U(ka, ca, kb, cb)                 \
+  do {                                             \
+    if ((kb) < (ka)) {                             \
+      float _t = (ka); (ka) = (kb); (kb) = _t;     \
+      int _c = (ca); (ca) = (cb); (cb) = _c;       \
+    }                                              \
+  } while (0)
 
-// Collects every leaf whose box meets Q into sm.leaves.  Returns the leaf
-// count, or -1 when a level or the leaf list exceeds its capacity.  All 32
-// lanes call it with the same Q.
-__device__ int gather_leaves(const IndexDev& ix, const float qlo[3], const float qhi[3], WarpSmem& sm) {
+// Exact 10-NN of every active lane's query (see header).  All 32 lanes call
+// it with warp-uniform control flow; inactive lanes only follow along.
+// Returns false if the stack bound was hit (cannot happen for depth <= MAX_LEVELS).
+__device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, float qz, KSet& L,
+                           WarpSmem& ps, unsigned long long& leaves) {
+  const unsigned FULL = 0xffffffffu;
+  const float INF = __int_as_float(0x7f800000);
   const int lane = threadIdx.x & 31;
-  int cur = 0;
-  int count = 1;
-  if (lane == 0) sm.front[0][0] = 0u;
-  __syncwarp();
-  for (int lvl = 0; lvl < ix.depth; ++lvl) {
-    const bool last = (lvl + 1 == ix.depth);
-    uint32_t* out = last ? sm.leaves : sm.front[cur ^ 1];
-    const int cap = last ? LEAF_CAP : FRONTIER_CAP;
-    int ncount = 0;
-    for (int b = 0; b < count; b += 32) {
-      int i = b + lane;
-      unsigned m4 = 0;
-      uint32_t j = 0;
-      if (i < count) {
-        j = sm.front[cur][i];
-        const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
-        float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
-        float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
-        float alx[4] = {lx.x, lx.y, lx.z, lx.w}, aly[4] = {ly.x, ly.y, ly.z, ly.w}, alz[4] = {lz.x, lz.y, lz.z, lz.w};
-        float ahx[4] = {hx.x, hx.y, hx.z, hx.w}, ahy[4] = {hy.x, hy.y, hy.z, hy.w}, ahz[4] = {hz.x, hz.y, hz.z, hz.w};
+  unsigned act = __ballot_sync(FULL, active);
+  if (act == 0 || ix.n <= 0) return true;
+  const int leader = __ffs(act) - 1;
+  int sp = 0;
+  int lvl = 0;
+  uint32_t j = 0;
+  while (true) {
+    const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
+    float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
+    float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
+    float bl[4][6] = {{lx.x, ly.x, lz.x, hx.x, hy.x, hz.x}, {lx.y, ly.y, lz.y, hx.y, hy.y, hz.y},
+                      {lx.z, ly.z, lz.z, hx.z, hy.z, hz.z}, {lx.w, ly.w, lz.w, hx.w, hy.w, hz.w}};
+    float m[4];
+    unsigned need[4];
+    float k[4];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          bool meet = alx[c] <= qhi[0] && ahx[c] >= qlo[0] && aly[c] <= qhi[1] && ahy[c] >= qlo[1] &&
-                      alz[c] <= qhi[2] && ahz[c] >= qlo[2];
-          m4 |= meet ? (1u << c) : 0u;
+    for (int c = 0; c < 4; ++c) {
+      m[c] = active ? d2_box(bl[c][0], bl[c][1], bl[c][2], bl[c][3], bl[c][4], bl[c][5], qx, qy, qz) : INF;
+      need[c] = __ballot_sync(FULL, active && m[c] <= L.wd);
+      k[c] = __shfl_sync(FULL, m[c], leader);
+    }
+    int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
+    float k0 = k[0], k1 = k[1], k2 = k[2], k3 = k[3];
+    RM_CSWAP_U(k0, o0, k1, o1);
+    RM_CSWAP_U(k2, o2, k3, o3);
+    RM_CSWAP_U(k0, o0, k2, o2);
+    RM_CSWAP_U(k1, o1, k3, o3);
+    RM_CSWAP_U(k1, o1, k2, o2);
+    // register arrays indexed by a runtime child number go through selects
+    auto pick_f = [](const float* a, int c) { return c == 0 ? a[0] : c == 1 ? a[1] : c == 2 ? a[2] : a[3]; };
+    auto pick_u = [](const unsigned* a, int c) { return c == 0 ? a[0] : c == 1 ? a[1] : c == 2 ? a[2] : a[3]; };
+    const uint32_t base = j * 4u;
+    if (lvl + 1 == ix.depth) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
+        if (!pick_u(need, c)) continue;
+        // bounds may have shrunk while scanning nearer leaves
+        if (!__ballot_sync(FULL, active && pick_f(m, c) <= L.wd)) continue;
+        int64_t start = (int64_t)(base + c) * ix.leaf;
+        int64_t end = start + ix.leaf;
+        if (end > ix.n) end = ix.n;
+        ++leaves;
+        for (int64_t i = start; i < end; ++i) {
+          float4 cr = __ldg(ix.rec + i);
+          if (active) {
+            float d = d2_point(cr, qx, qy, qz);
+            if (d <= L.wd) L.consider(d, (int32_t)i, cr.w, ix.perm);
+          }
         }
       }
-      int n = __popc(m4);
-      int incl = n;
+    } else {
+      // push the needed children farthest-first, descend into the nearest
+      int first = -1;
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += t;
+      for (int t = 0; t < 4; ++t) {
+        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
+        if (pick_u(need, c) && first < 0) first = c;
       }
-      int total = __shfl_sync(0xffffffffu, incl, 31);
-      if (ncount + total > cap) return -1;
-      int w = ncount + incl - n;
+      if (sp + 3 > PSTACK) return false;
+      const uint32_t code = (uint32_t)(lvl + 1) << 28;
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (m4 & (1u << c)) out[w++] = j * 4u + (uint32_t)c;
-      ncount += total;
+      for (int t = 3; t >= 0; --t) {
+        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
+        if (pick_u(need, c) && c != first) {
+          if (lane == 0) {
+            ps.code[sp] = code | (base + c);
+            const float* b0 = bl[0];
+            const float* b1 = bl[1];
+            const float* b2 = bl[2];
+            const float* b3 = bl[3];
+#pragma unroll
+            for (int e = 0; e < 6; ++e)
+              ps.box[sp][e] = c == 0 ? b0[e] : c == 1 ? b1[e] : c == 2 ? b2[e] : b3[e];
+          }
+          ++sp;
+        }
+      }
+      __syncwarp();
+      if (first >= 0) {
+        lvl = lvl + 1;
+        j = base + first;
+        continue;
+      }
     }
-    __syncwarp();
-    if (last) return ncount;
-    if (ncount == 0) return 0;
-    cur ^= 1;
-    count = ncount;
-  }
-  return 0;
-}
-
-// Stages the records of the gathered leaves and lets every `member` lane
-// consider every staged point.  All lanes call it.
-__device__ void scan_gathered(const IndexDev& ix, WarpSmem& sm, int nleaves, bool member, float px,
-                              float py, float pz, KSet& L) {
-  const int lane = threadIdx.x & 31;
-  const int leaf = ix.leaf;
-  const int per_round = STAGE_CAP / leaf;  // whole leaves per staging round
-  for (int l0 = 0; l0 < nleaves; l0 += per_round) {
-    int nl = min(per_round, nleaves - l0);
-    int slots = nl * leaf;
-    __syncwarp();
-    for (int k = lane; k < slots; k += 32) {
-      int li = k / leaf, o = k - li * leaf;
-      int64_t p = (int64_t)sm.leaves[l0 + li] * leaf + o;
-      if (p < ix.n) {
-        sm.rec[k] = __ldg(ix.rec + p);
-        sm.pos[k] = (int32_t)p;
-      } else {
-        sm.rec[k] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
-        sm.pos[k] = -1;
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      float md = active ? d2_box(ps.box[sp][0], ps.box[sp][1], ps.box[sp][2], ps.box[sp][3],
+                                 ps.box[sp][4], ps.box[sp][5], qx, qy, qz)
+                        : INF;
+      if (__ballot_sync(FULL, active && md <= L.wd)) {
+        uint32_t code = ps.code[sp];
+        lvl = (int)(code >> 28);
+        j = code & 0x0fffffffu;
+        found = true;
+        break;
       }
     }
     __syncwarp();
-    if (member) {
-      for (int k = 0; k < slots; ++k) {
-        float4 c = sm.rec[k];
-        float d = d2_point(c, px, py, pz);
-        if (d <= L.wd && sm.pos[k] >= 0) L.consider(d, sm.pos[k], c.w, ix.perm);
-      }
-    }
+    if (!found) break;
   }
-  __syncwarp();
+  return true;
 }
 
 __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs& v, int64_t pix, int32_t s,
@@ -270,35 +289,14 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
     float py = __fmaf_rn(r.dy, t, r.oy);
     float pz = __fmaf_rn(r.dz, t, r.oz);
     if (stepping) L.rewarm(ix, px, py, pz);
-    bool member = stepping && L.wd <= mp.coop_r2;
-    unsigned mm = __ballot_sync(FULL, member);
-    bool done = false;
-    if (__popc(mm) >= 2) {
-      // Q: box of the members' balls; the radius is rounded outwards so that
-      // every point whose computed d2 is <= wd lies inside
-      float rad = member ? __fmul_rn(__fsqrt_rn(L.wd), 1.0f + 1e-5f) + 1e-5f : 0.0f;
-      float qlo[3], qhi[3];
-      qlo[0] = warp_min(member ? px - rad : INFINITY);
-      qlo[1] = warp_min(member ? py - rad : INFINITY);
-      qlo[2] = warp_min(member ? pz - rad : INFINITY);
-      qhi[0] = warp_max(member ? px + rad : -INFINITY);
-      qhi[1] = warp_max(member ? py + rad : -INFINITY);
-      qhi[2] = warp_max(member ? pz + rad : -INFINITY);
-      int nl = gather_leaves(ix, qlo, qhi, sm);
-      if (nl >= 0) {
-        scan_gathered(ix, sm, nl, member, px, py, pz, L);
-        done = member;
-      } else {
-        cnt.overflow += (lane == 0) ? 1 : 0;
-      }
+    if (mp.search == 1) {
+      if (!packet_knn(ix, stepping, px, py, pz, L, sm, cnt.leaves)) cnt.bad += stepping ? 1 : 0;
+    } else if (stepping) {
+      if (!knn_search(ix, px, py, pz, L)) cnt.bad += 1;
     }
     if (stepping) {
-      if (!done) {
-        if (!knn_search(ix, px, py, pz, L)) cnt.bad += 1;
-        cnt.solo += 1;
-      } else {
-        cnt.coop += 1;
-      }
+      if (mp.search == 1) cnt.coop += 1;
+      else cnt.solo += 1;
       int32_t s;
       float step = L.step_value(ix.perm, &s);
       ++nsteps;
@@ -325,7 +323,7 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
 }
 
 __device__ __forceinline__ void flush_counters(LaneCounters& c, unsigned long long* counters) {
-  unsigned long long v[7] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.overflow};
+  unsigned long long v[7] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.leaves};
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
 #pragma unroll
@@ -349,7 +347,7 @@ struct PlainArgs {
 };
 
 // One warp per 8x4 tile.
-__global__ void __launch_bounds__(32 * WARPS_PER_CTA)
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA, 2)
 k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
   const int warp = threadIdx.x >> 5;
@@ -400,7 +398,7 @@ __device__ __forceinline__ int find_view(const ViewDev* views, int n, int64_t it
   return lo;
 }
 
-__global__ void __launch_bounds__(32 * WARPS_PER_CTA)
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA, 2)
 k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __restrict__ queue,
               unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
@@ -454,8 +452,7 @@ static ClipBox clip_box(const Ctx& c, float max_r) {
 static MarchParams march_params(const Ctx& c) {
   MarchParams mp;
   mp.clip = clip_box(c, c.max_r);
-  float cr = c.coop_radius;
-  mp.coop_r2 = cr * cr;
+  mp.search = c.launch.search;
   return mp;
 }
 

@@ -248,15 +248,15 @@ class Renderer:
         self._check(self._lib.rm_render_batch(self._h, cviews, len(views), frames,
                                               _abi.RM_DEVICE if device else _abi.RM_HOST))
 
-    def set_launch(self, tile_w=8, tile_h=4, rays_per_lane=1, ctas_per_sm=4, coop_radius=0.03):
-        L = _abi.RmLaunch(tile_w, tile_h, rays_per_lane, ctas_per_sm, coop_radius)
+    def set_launch(self, tile_w=8, tile_h=4, rays_per_lane=1, ctas_per_sm=4, search=1):
+        L = _abi.RmLaunch(tile_w, tile_h, rays_per_lane, ctas_per_sm, search)
         self._check(self._lib.rm_set_launch(self._h, ctypes.byref(L)))
 
     def get_launch(self) -> dict:
         L = _abi.RmLaunch()
         self._check(self._lib.rm_get_launch(self._h, ctypes.byref(L)))
         return {"tile_w": L.tile_w, "tile_h": L.tile_h, "rays_per_lane": L.rays_per_lane,
-                "ctas_per_sm": L.ctas_per_sm, "coop_radius": round(L.coop_radius, 6)}
+                "ctas_per_sm": L.ctas_per_sm, "search": L.search}
 
     def autotune(self, views) -> dict:
         arr = (_abi.RmView * len(views))(*[v.to_c() for v in views])
@@ -266,15 +266,14 @@ class Renderer:
         self._check(self._lib.rm_autotune(self._h, arr, len(views), ctypes.byref(L), ctypes.byref(leaf),
                                           ctypes.byref(ms)))
         return {"tile_w": L.tile_w, "tile_h": L.tile_h, "rays_per_lane": L.rays_per_lane,
-                "ctas_per_sm": L.ctas_per_sm, "coop_radius": round(L.coop_radius, 6),
+                "ctas_per_sm": L.ctas_per_sm, "search": L.search,
                 "leaf_size": leaf.value, "ms": round(ms.value, 3)}
 
     def stats(self) -> dict:
         s = _abi.RmStats()
         self._check(self._lib.rm_get_stats(self._h, ctypes.byref(s)))
-        return {"rays": s.rays, "steps": s.steps, "hits": s.hits, "coop_steps": s.coop_steps,
-                "solo_steps": s.solo_steps, "gather_overflows": s.gather_overflows,
-                "kernel_ms": s.kernel_ms}
+        return {"rays": s.rays, "steps": s.steps, "hits": s.hits, "packet_steps": s.packet_steps,
+                "solo_steps": s.solo_steps, "packet_leaves": s.packet_leaves, "kernel_ms": s.kernel_ms}
 
     # -- backward -------------------------------------------------------------
     def backward(self, views, dl_drgb, dl_ddepth, hit, g_rgb, g_xyz, g_radius):

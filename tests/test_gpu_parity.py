@@ -116,7 +116,7 @@ def test_render_batch_equals_plain(scene100k):
     specs = syn.make_views(6, seed=9, boxes=sc.boxes, resolutions=[(160, 120), (213, 138), (96, 54)])
     views = views_from_specs(specs)
     plain = [r.render(v, outputs=("rgbd", "hit", "depth", "steps")) for v in views]
-    for launch in [(8, 4, 1, 4, 0.03), (8, 4, 2, 4, 0.0), (4, 8, 4, 2, 0.06), (16, 2, 2, 8, 0.015)]:
+    for launch in [(8, 4, 1, 4, 1), (8, 4, 2, 4, 0), (4, 8, 4, 2, 1), (16, 2, 2, 8, 1)]:
         r.set_launch(*launch)
         batch = r.render_batch(views, outputs=("rgbd", "hit", "depth", "steps"), device=False)
         for p, b in zip(plain, batch):
