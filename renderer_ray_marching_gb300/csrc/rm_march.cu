@@ -70,15 +70,8 @@ __device__ __forceinline__ float clip_exit(const Ray& r, const ClipBox& e) {
   return tmax + fabsf(tmax) * 1e-5f + 1e-3f;
 }
 
-// Per-warp shared memory of the packet traversal: the stack of pending
-// nodes with their boxes (re-tested when popped).
 constexpr int WARPS_PER_CTA = 4;
-constexpr int PSTACK = 3 * MAX_LEVELS + 4;
-
-struct WarpSmem {
-  uint32_t code[PSTACK];
-  float box[PSTACK][6];
-};
+using WarpSmem = PacketStack;
 
 struct MarchParams {
   ClipBox clip;
@@ -101,127 +94,6 @@ struct ViewArgs {
 struct LaneCounters {
   unsigned long long steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0;
 };
-
-#define RM_CSWAP_U(ka, ca, kb, cb)                 \
-  do {                                             \
-    if ((kb) < (ka)) {                             \
-      float _t = (ka); (ka) = (kb); (kb) = _t;     \
-      int _c = (ca); (ca) = (cb); (cb) = _c;       \
-    }                                              \
-  } while (0)
-
-// Exact 10-NN of every active lane's query (see header).  All 32 lanes call
-// it with warp-uniform control flow; inactive lanes only follow along.
-// Returns false if the stack bound was hit (cannot happen for depth <= MAX_LEVELS).
-__device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, float qz, KSet& L,
-                           WarpSmem& ps, unsigned long long& leaves) {
-  const unsigned FULL = 0xffffffffu;
-  const float INF = __int_as_float(0x7f800000);
-  const int lane = threadIdx.x & 31;
-  unsigned act = __ballot_sync(FULL, active);
-  if (act == 0 || ix.n <= 0) return true;
-  const int leader = __ffs(act) - 1;
-  int sp = 0;
-  int lvl = 0;
-  uint32_t j = 0;
-  while (true) {
-    const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
-    float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
-    float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
-    float bl[4][6] = {{lx.x, ly.x, lz.x, hx.x, hy.x, hz.x}, {lx.y, ly.y, lz.y, hx.y, hy.y, hz.y},
-                      {lx.z, ly.z, lz.z, hx.z, hy.z, hz.z}, {lx.w, ly.w, lz.w, hx.w, hy.w, hz.w}};
-    float m[4];
-    unsigned need[4];
-    float k[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      m[c] = active ? d2_box(bl[c][0], bl[c][1], bl[c][2], bl[c][3], bl[c][4], bl[c][5], qx, qy, qz) : INF;
-      need[c] = __ballot_sync(FULL, active && m[c] <= L.wd);
-      k[c] = __shfl_sync(FULL, m[c], leader);
-    }
-    int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
-    float k0 = k[0], k1 = k[1], k2 = k[2], k3 = k[3];
-    RM_CSWAP_U(k0, o0, k1, o1);
-    RM_CSWAP_U(k2, o2, k3, o3);
-    RM_CSWAP_U(k0, o0, k2, o2);
-    RM_CSWAP_U(k1, o1, k3, o3);
-    RM_CSWAP_U(k1, o1, k2, o2);
-    // register arrays indexed by a runtime child number go through selects
-    auto pick_f = [](const float* a, int c) { return c == 0 ? a[0] : c == 1 ? a[1] : c == 2 ? a[2] : a[3]; };
-    auto pick_u = [](const unsigned* a, int c) { return c == 0 ? a[0] : c == 1 ? a[1] : c == 2 ? a[2] : a[3]; };
-    const uint32_t base = j * 4u;
-    if (lvl + 1 == ix.depth) {
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
-        if (!pick_u(need, c)) continue;
-        // bounds may have shrunk while scanning nearer leaves
-        if (!__ballot_sync(FULL, active && pick_f(m, c) <= L.wd)) continue;
-        int64_t start = (int64_t)(base + c) * ix.leaf;
-        int64_t end = start + ix.leaf;
-        if (end > ix.n) end = ix.n;
-        ++leaves;
-        for (int64_t i = start; i < end; ++i) {
-          float4 cr = __ldg(ix.rec + i);
-          if (active) {
-            float d = d2_point(cr, qx, qy, qz);
-            if (d <= L.wd) L.consider(d, (int32_t)i, cr.w, ix.perm);
-          }
-        }
-      }
-    } else {
-      // push the needed children farthest-first, descend into the nearest
-      int first = -1;
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
-        if (pick_u(need, c) && first < 0) first = c;
-      }
-      if (sp + 3 > PSTACK) return false;
-      const uint32_t code = (uint32_t)(lvl + 1) << 28;
-#pragma unroll
-      for (int t = 3; t >= 0; --t) {
-        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
-        if (pick_u(need, c) && c != first) {
-          if (lane == 0) {
-            ps.code[sp] = code | (base + c);
-            const float* b0 = bl[0];
-            const float* b1 = bl[1];
-            const float* b2 = bl[2];
-            const float* b3 = bl[3];
-#pragma unroll
-            for (int e = 0; e < 6; ++e)
-              ps.box[sp][e] = c == 0 ? b0[e] : c == 1 ? b1[e] : c == 2 ? b2[e] : b3[e];
-          }
-          ++sp;
-        }
-      }
-      __syncwarp();
-      if (first >= 0) {
-        lvl = lvl + 1;
-        j = base + first;
-        continue;
-      }
-    }
-    bool found = false;
-    while (sp > 0) {
-      --sp;
-      float md = active ? d2_box(ps.box[sp][0], ps.box[sp][1], ps.box[sp][2], ps.box[sp][3],
-                                 ps.box[sp][4], ps.box[sp][5], qx, qy, qz)
-                        : INF;
-      if (__ballot_sync(FULL, active && md <= L.wd)) {
-        uint32_t code = ps.code[sp];
-        lvl = (int)(code >> 28);
-        j = code & 0x0fffffffu;
-        found = true;
-        break;
-      }
-    }
-    __syncwarp();
-    if (!found) break;
-  }
-  return true;
-}
 
 __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs& v, int64_t pix, int32_t s,
                                              float depth, int32_t steps) {
