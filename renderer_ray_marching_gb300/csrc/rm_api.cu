@@ -688,7 +688,7 @@ rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* c
       float t = time_once(L);
       if (t < best_t) { best_t = t; best_l = L; }
     }
-    for (int ctas : {2, 8}) {
+    for (int ctas : {2, 6, 8}) {
       rm_launch L = best_l;
       L.ctas_per_sm = ctas;
       float t = time_once(L);

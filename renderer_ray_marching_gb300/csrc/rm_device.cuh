@@ -113,15 +113,16 @@ __device__ __forceinline__ float klist_worst(const KList<K>& L) {
 }
 
 // The marcher's 10 nearest, kept as an unsorted set with its worst entry
-// (largest (d2, cloud index)) tracked: an insertion replaces the worst slot,
-// and re-seeding at the next step's position re-measures the ten points
-// without sorting.  Insertions skip points already present, so the set can
-// start from the previous step's points (they are valid candidates: the
-// search then prunes with a finite bound from the first node and stays exact).
+// (largest (d2, cloud index)) tracked: an insertion replaces the worst slot
+// and the new worst comes from a 4-level reduction tree; re-seeding at the
+// next step's position re-measures the ten points without sorting.
+// Insertions skip points already present, so the set can start from the
+// previous step's points (they are valid candidates: the search then prunes
+// with a finite bound from the first node and stays exact).  Radii are not
+// kept here; the step value reads them from the records.
 struct KSet {
   float d[KNN];
   int32_t s[KNN];   // sorted position, -1 = empty
-  float r[KNN];
   float wd;         // worst entry: d2, position, slot
   int32_t ws;
   int wi;
@@ -131,32 +132,53 @@ struct KSet {
     for (int j = 0; j < KNN; ++j) {
       d[j] = __int_as_float(0x7f800000);
       s[j] = -1;
-      r[j] = 0.0f;
     }
     wd = __int_as_float(0x7f800000);
     ws = -1;
     wi = 0;
   }
 
+  // (da, sa) after (db, sb) in (d2, cloud index) order; empty slots are last.
+  static __device__ __forceinline__ bool later(float da, int32_t sa, float db, int32_t sb,
+                                               const int32_t* __restrict__ perm) {
+    if (da != db) return da > db;
+    if (sb < 0) return false;
+    if (sa < 0) return true;
+    return __ldg(perm + sa) > __ldg(perm + sb);
+  }
+
   __device__ __forceinline__ void recompute_worst(const int32_t* __restrict__ perm) {
-    wd = d[0];
-    ws = s[0];
-    wi = 0;
+    float td[KNN / 2];
+    int32_t ts[KNN / 2];
+    int ti[KNN / 2];
 #pragma unroll
-    for (int j = 1; j < KNN; ++j) {
-      bool later = d[j] > wd;
-      if (!later && d[j] == wd && ws >= 0) later = s[j] < 0 || __ldg(perm + s[j]) > __ldg(perm + ws);
-      if (later) {
-        wd = d[j];
-        ws = s[j];
-        wi = j;
-      }
+    for (int p = 0; p < KNN / 2; ++p) {
+      bool a = later(d[2 * p], s[2 * p], d[2 * p + 1], s[2 * p + 1], perm);
+      td[p] = a ? d[2 * p] : d[2 * p + 1];
+      ts[p] = a ? s[2 * p] : s[2 * p + 1];
+      ti[p] = a ? 2 * p : 2 * p + 1;
     }
+    // 5 -> 2 (+1) -> 1
+    bool a01 = later(td[0], ts[0], td[1], ts[1], perm);
+    float d01 = a01 ? td[0] : td[1];
+    int32_t s01 = a01 ? ts[0] : ts[1];
+    int i01 = a01 ? ti[0] : ti[1];
+    bool a23 = later(td[2], ts[2], td[3], ts[3], perm);
+    float d23 = a23 ? td[2] : td[3];
+    int32_t s23 = a23 ? ts[2] : ts[3];
+    int i23 = a23 ? ti[2] : ti[3];
+    bool a03 = later(d01, s01, d23, s23, perm);
+    float d03 = a03 ? d01 : d23;
+    int32_t s03 = a03 ? s01 : s23;
+    int i03 = a03 ? i01 : i23;
+    bool a4 = later(d03, s03, td[4], ts[4], perm);
+    wd = a4 ? d03 : td[4];
+    ws = a4 ? s03 : ts[4];
+    wi = a4 ? i03 : ti[4];
   }
 
   // Candidate (dd, ss) with dd <= wd.
-  __device__ __forceinline__ void consider(float dd, int32_t ss, float rr,
-                                           const int32_t* __restrict__ perm) {
+  __device__ __forceinline__ void consider(float dd, int32_t ss, const int32_t* __restrict__ perm) {
     if (dd == wd && ws >= 0 && !(__ldg(perm + ss) < __ldg(perm + ws))) return;
     bool dup = false;
 #pragma unroll
@@ -167,7 +189,6 @@ struct KSet {
       if (j == wi) {
         d[j] = dd;
         s[j] = ss;
-        r[j] = rr;
       }
     }
     recompute_worst(perm);
@@ -184,16 +205,16 @@ struct KSet {
   // src/ray_marching.cu:280-290: min of sqrtf(d2) - r visiting candidates
   // in ascending (d2, index) order with a strict "<" -- equivalently the
   // minimum value, ties going to the smaller (d2, index).
-  __device__ __forceinline__ float step_value(const int32_t* __restrict__ perm, int32_t* best_s) const {
+  __device__ __forceinline__ float step_value(const IndexDev& ix, int32_t* best_s) const {
     float best = __int_as_float(0x7f800000), bd = best;
     int32_t bs = -1;
 #pragma unroll
     for (int j = 0; j < KNN; ++j) {
       if (s[j] >= 0) {
-        float v = __fsub_rn(__fsqrt_rn(d[j]), r[j]);
+        float v = __fsub_rn(__fsqrt_rn(d[j]), __ldg(&ix.rec[s[j]].w));
         bool take = v < best;
         if (!take && v == best)
-          take = d[j] < bd || (d[j] == bd && __ldg(perm + s[j]) < __ldg(perm + bs));
+          take = d[j] < bd || (d[j] == bd && __ldg(ix.perm + s[j]) < __ldg(ix.perm + bs));
         if (take) {
           best = v;
           bd = d[j];
@@ -210,7 +231,8 @@ __device__ __forceinline__ float list_worst(const KSet& L) { return L.wd; }
 template <int K>
 __device__ __forceinline__ float list_worst(const KList<K>& L) { return L.d[K - 1]; }
 __device__ __forceinline__ void list_consider(KSet& L, float d, int32_t s, float r, const int32_t* perm) {
-  L.consider(d, s, r, perm);
+  (void)r;
+  L.consider(d, s, perm);
 }
 template <int K>
 __device__ __forceinline__ void list_consider(KList<K>& L, float d, int32_t s, float r, const int32_t* perm) {
@@ -305,17 +327,17 @@ __device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, Lis
   return true;
 }
 
-// Per-warp shared memory of a packet traversal: pending nodes with their
-// boxes (re-tested when popped).
+// Per-warp shared memory of a packet traversal: pending nodes (their boxes
+// are re-read from the parent's group and re-tested when popped).
 constexpr int PSTACK = 3 * MAX_LEVELS + 4;
 struct PacketStack {
   uint32_t code[PSTACK];
-  float box[PSTACK][6];
 };
 
 __device__ __forceinline__ void list_consider_unique(KSet& L, float d, int32_t s, float r,
                                                      const int32_t* perm) {
-  L.consider(d, s, r, perm);
+  (void)r;
+  L.consider(d, s, perm);
 }
 template <int K>
 __device__ __forceinline__ void list_consider_unique(KList<K>& L, float d, int32_t s, float r,
@@ -346,7 +368,7 @@ __device__ __forceinline__ void list_consider_unique(KList<K>& L, float d, int32
 // if the stack bound was hit (cannot happen for depth <= MAX_LEVELS).
 template <class List>
 __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, float qz, List& L,
-                           PacketStack& ps, unsigned long long& leaves) {
+                           PacketStack& ps, unsigned& leaves) {
   const unsigned FULL = 0xffffffffu;
   const float INF = __int_as_float(0x7f800000);
   const int lane = threadIdx.x & 31;
@@ -358,37 +380,37 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   uint32_t j = 0;
   while (true) {
     const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
-    float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
-    float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
-    float bl[4][6] = {{lx.x, ly.x, lz.x, hx.x, hy.x, hz.x}, {lx.y, ly.y, lz.y, hx.y, hy.y, hz.y},
-                      {lx.z, ly.z, lz.z, hx.z, hy.z, hz.z}, {lx.w, ly.w, lz.w, hx.w, hy.w, hz.w}};
-    float m[4];
-    unsigned need[4];
-    float k[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      m[c] = active ? d2_box(bl[c][0], bl[c][1], bl[c][2], bl[c][3], bl[c][4], bl[c][5], qx, qy, qz) : INF;
-      need[c] = __ballot_sync(FULL, active && m[c] <= list_worst(L));
-      k[c] = __shfl_sync(FULL, m[c], leader);
+    float m0, m1, m2, m3;
+    {
+      float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
+      float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
+      m0 = active ? d2_box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, qx, qy, qz) : INF;
+      m1 = active ? d2_box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, qx, qy, qz) : INF;
+      m2 = active ? d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz) : INF;
+      m3 = active ? d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz) : INF;
     }
+    const float w = list_worst(L);
+    const unsigned n0 = __ballot_sync(FULL, m0 <= w), n1 = __ballot_sync(FULL, m1 <= w);
+    const unsigned n2 = __ballot_sync(FULL, m2 <= w), n3 = __ballot_sync(FULL, m3 <= w);
+    float k0 = __shfl_sync(FULL, m0, leader), k1 = __shfl_sync(FULL, m1, leader);
+    float k2 = __shfl_sync(FULL, m2, leader), k3 = __shfl_sync(FULL, m3, leader);
     int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
-    float k0 = k[0], k1 = k[1], k2 = k[2], k3 = k[3];
     RM_CSWAP_U(k0, o0, k1, o1);
     RM_CSWAP_U(k2, o2, k3, o3);
     RM_CSWAP_U(k0, o0, k2, o2);
     RM_CSWAP_U(k1, o1, k3, o3);
     RM_CSWAP_U(k1, o1, k2, o2);
-    // register arrays indexed by a runtime child number go through selects
-    auto pick_f = [](const float* a, int c) { return c == 0 ? a[0] : c == 1 ? a[1] : c == 2 ? a[2] : a[3]; };
-    auto pick_u = [](const unsigned* a, int c) { return c == 0 ? a[0] : c == 1 ? a[1] : c == 2 ? a[2] : a[3]; };
+    // 4-bit mask of the needed children (warp-uniform)
+    const unsigned needm = (n0 ? 1u : 0u) | (n1 ? 2u : 0u) | (n2 ? 4u : 0u) | (n3 ? 8u : 0u);
     const uint32_t base = j * 4u;
     if (lvl + 1 == ix.depth) {
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
-        if (!pick_u(need, c)) continue;
+        if (!(needm & (1u << c))) continue;
         // bounds may have shrunk while scanning nearer leaves
-        if (!__ballot_sync(FULL, active && pick_f(m, c) <= list_worst(L))) continue;
+        const float mc = c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3;
+        if (!__ballot_sync(FULL, mc <= list_worst(L))) continue;
         int64_t start = (int64_t)(base + c) * ix.leaf;
         int64_t end = start + ix.leaf;
         if (end > ix.n) end = ix.n;
@@ -407,24 +429,15 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
-        if (pick_u(need, c) && first < 0) first = c;
+        if ((needm & (1u << c)) && first < 0) first = c;
       }
       if (sp + 3 > PSTACK) return false;
       const uint32_t code = (uint32_t)(lvl + 1) << 28;
 #pragma unroll
       for (int t = 3; t >= 0; --t) {
         const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
-        if (pick_u(need, c) && c != first) {
-          if (lane == 0) {
-            ps.code[sp] = code | (base + c);
-            const float* b0 = bl[0];
-            const float* b1 = bl[1];
-            const float* b2 = bl[2];
-            const float* b3 = bl[3];
-#pragma unroll
-            for (int e = 0; e < 6; ++e)
-              ps.box[sp][e] = c == 0 ? b0[e] : c == 1 ? b1[e] : c == 2 ? b2[e] : b3[e];
-          }
+        if ((needm & (1u << c)) && c != first) {
+          if (lane == 0) ps.code[sp] = code | (base + c);
           ++sp;
         }
       }
@@ -438,13 +451,20 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
     bool found = false;
     while (sp > 0) {
       --sp;
-      float md = active ? d2_box(ps.box[sp][0], ps.box[sp][1], ps.box[sp][2], ps.box[sp][3],
-                                 ps.box[sp][4], ps.box[sp][5], qx, qy, qz)
-                        : INF;
-      if (__ballot_sync(FULL, active && md <= list_worst(L))) {
-        uint32_t code = ps.code[sp];
-        lvl = (int)(code >> 28);
-        j = code & 0x0fffffffu;
+      const uint32_t code = ps.code[sp];
+      const int plvl = (int)(code >> 28);
+      const uint32_t pj = code & 0x0fffffffu;
+      // the node's box: lane (pj & 3) of its parent's group
+      const float* pg = reinterpret_cast<const float*>(
+          ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(plvl - 1) + (pj >> 2)));
+      const int c = (int)(pj & 3u);
+      float md = INF;
+      if (active)
+        md = d2_box(__ldg(pg + 0 + c), __ldg(pg + 4 + c), __ldg(pg + 8 + c), __ldg(pg + 12 + c),
+                    __ldg(pg + 16 + c), __ldg(pg + 20 + c), qx, qy, qz);
+      if (__ballot_sync(FULL, md <= list_worst(L))) {
+        lvl = plvl;
+        j = pj;
         found = true;
         break;
       }
@@ -454,7 +474,6 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   }
   return true;
 }
-
 
 // ---------------------------------------------------------------------------
 // Camera rays, src/ray_marching.cu:70-79.

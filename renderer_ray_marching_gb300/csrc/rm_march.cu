@@ -92,7 +92,7 @@ struct ViewArgs {
 // counters: [0] steps, [1] rays, [2] hits, [3] search errors,
 //           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets
 struct LaneCounters {
-  unsigned long long steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0;
+  unsigned steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0;
 };
 
 __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs& v, int64_t pix, int32_t s,
@@ -112,7 +112,8 @@ __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs&
 }
 
 // Marches every ray of one item (origin x0, y0; tile_w x tile_h*rpl pixels)
-// of view v.  All 32 lanes call it.
+// of view v.  All 32 lanes call it.  SEARCH: 1 packet traversal, 0 per lane.
+template <int SEARCH>
 __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0, int tile_w,
                            int tile_h, int rpl, const MarchParams& mp, WarpSmem& sm, LaneCounters& cnt) {
   const unsigned FULL = 0xffffffffu;
@@ -161,16 +162,16 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
     float py = __fmaf_rn(r.dy, t, r.oy);
     float pz = __fmaf_rn(r.dz, t, r.oz);
     if (stepping) L.rewarm(ix, px, py, pz);
-    if (mp.search == 1) {
+    if (SEARCH == 1) {
       if (!packet_knn(ix, stepping, px, py, pz, L, sm, cnt.leaves)) cnt.bad += stepping ? 1 : 0;
     } else if (stepping) {
       if (!knn_search(ix, px, py, pz, L)) cnt.bad += 1;
     }
     if (stepping) {
-      if (mp.search == 1) cnt.coop += 1;
+      if (SEARCH == 1) cnt.coop += 1;
       else cnt.solo += 1;
       int32_t s;
-      float step = L.step_value(ix.perm, &s);
+      float step = L.step_value(ix, &s);
       ++nsteps;
       t = __fadd_rn(t, step);
       bool fin = false;
@@ -195,7 +196,7 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
 }
 
 __device__ __forceinline__ void flush_counters(LaneCounters& c, unsigned long long* counters) {
-  unsigned long long v[7] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.leaves};
+  unsigned long long v[7] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.leaves};  // widened
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
 #pragma unroll
@@ -218,8 +219,10 @@ struct PlainArgs {
   int32_t* steps;
 };
 
-// One warp per 8x4 tile.
-__global__ void __launch_bounds__(32 * WARPS_PER_CTA, 2)
+// One warp per 8x4 tile.  MINB: CTAs per SM the register budget is sized
+// for (the launch's ctas_per_sm picks the instance).
+template <int SEARCH, int MINB>
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA, MINB)
 k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
   const int warp = threadIdx.x >> 5;
@@ -237,7 +240,7 @@ k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __re
     v.hit = a.hit;
     v.depth = a.depth;
     v.steps = a.steps;
-    march_item(ix, v, (tile % tiles_x) * 8, (tile / tiles_x) * 4, 8, 4, 1, mp, smem[warp], cnt);
+    march_item<SEARCH>(ix, v, (tile % tiles_x) * 8, (tile / tiles_x) * 4, 8, 4, 1, mp, smem[warp], cnt);
   }
   flush_counters(cnt, counters);
 }
@@ -270,7 +273,8 @@ __device__ __forceinline__ int find_view(const ViewDev* views, int n, int64_t it
   return lo;
 }
 
-__global__ void __launch_bounds__(32 * WARPS_PER_CTA, 2)
+template <int SEARCH, int MINB>
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA, MINB)
 k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __restrict__ queue,
               unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
@@ -295,7 +299,7 @@ k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __re
     v.steps = V.steps;
     int x0 = (int)(local % V.tiles_x) * a.tile_w;
     int y0 = (int)(local / V.tiles_x) * (a.tile_h * a.rpl);
-    march_item(ix, v, x0, y0, a.tile_w, a.tile_h, a.rpl, mp, smem[warp], cnt);
+    march_item<SEARCH>(ix, v, x0, y0, a.tile_w, a.tile_h, a.rpl, mp, smem[warp], cnt);
   }
   flush_counters(cnt, counters);
 }
@@ -345,7 +349,16 @@ void launch_render_plain(Ctx& c, const rm_view& v, float4* rgbd, int32_t* hit, f
   a.steps = steps;
   int64_t tiles = (int64_t)((v.width + 7) / 8) * ((v.height + 3) / 4);
   unsigned grid = (unsigned)((tiles + WARPS_PER_CTA - 1) / WARPS_PER_CTA);
-  k_march_plain<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, march_params(c), counters);
+  MarchParams mp = march_params(c);
+  auto go = [&](auto kern) { kern<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, mp, counters); };
+  const int cps = c.launch.ctas_per_sm;
+  if (mp.search == 1) {
+    if (cps >= 8) go(k_march_plain<1, 8>);
+    else if (cps >= 6) go(k_march_plain<1, 6>);
+    else go(k_march_plain<1, 4>);
+  } else {
+    go(k_march_plain<0, 4>);
+  }
 }
 
 void launch_prepare_views(Ctx& c, ViewDev* views_dev, int n, unsigned long long* counters) {
@@ -364,7 +377,18 @@ void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
   a.rpl = L.rays_per_lane;
   unsigned long long* queue = c.queue.ptr<unsigned long long>();
   int grid = c.sm_count * (L.ctas_per_sm > 0 ? L.ctas_per_sm : 4);
-  k_march_batch<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, march_params(c), queue, counters);
+  MarchParams mp = march_params(c);
+  auto go = [&](auto kern) {
+    kern<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, mp, queue, counters);
+  };
+  const int cps = L.ctas_per_sm;
+  if (mp.search == 1) {
+    if (cps >= 8) go(k_march_batch<1, 8>);
+    else if (cps >= 6) go(k_march_batch<1, 6>);
+    else go(k_march_batch<1, 4>);
+  } else {
+    go(k_march_batch<0, 4>);
+  }
 }
 
 }  // namespace rm

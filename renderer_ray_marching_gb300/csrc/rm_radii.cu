@@ -41,7 +41,7 @@ k_radii_packet(IndexDev ix, float max_radius, float* __restrict__ radii_out, int
   __shared__ PacketStack stacks[RADII_WARPS];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t nwarps = (int64_t)gridDim.x * RADII_WARPS;
-  unsigned long long leaves = 0;
+  unsigned leaves = 0;
   for (int64_t wbase = ((int64_t)blockIdx.x * RADII_WARPS + warp) * 32; wbase < ix.n; wbase += nwarps * 32) {
     const int64_t s = wbase + lane;
     const bool active = s < ix.n;

@@ -20,8 +20,9 @@ def scene100k():
     return sc, ix
 
 
-def make_renderer(xyz, rgb=None, leaf=16, max_radius=0.1):
+def make_renderer(xyz, rgb=None, leaf=16, max_radius=0.1, search=1):
     r = Renderer(leaf_size=leaf)
+    r.set_launch(search=search)
     r.set_cloud(xyz, rgb)
     r.build_index()
     radii, nn = r.compute_radii(max_radius)
@@ -59,10 +60,10 @@ def test_knn_empty_cloud_pads():
     assert np.all(gi == -1) and np.all(np.isinf(gd))
 
 
-@pytest.mark.parametrize("leaf", [8, 16, 32])
-def test_radii_bit_exact(scene100k, leaf):
+@pytest.mark.parametrize("leaf,search", [(8, 1), (16, 1), (32, 1), (16, 0)])
+def test_radii_bit_exact(scene100k, leaf, search):
     sc, ix = scene100k
-    r, radii, nn = make_renderer(sc.xyz, sc.rgb, leaf=leaf)
+    r, radii, nn = make_renderer(sc.xyz, sc.rgb, leaf=leaf, search=search)
     orad, onn = ix.radii(0.0)
     assert np.array_equal(radii.view(np.int32), orad.view(np.int32))
     assert np.array_equal(nn, onn)
@@ -116,7 +117,7 @@ def test_render_batch_equals_plain(scene100k):
     specs = syn.make_views(6, seed=9, boxes=sc.boxes, resolutions=[(160, 120), (213, 138), (96, 54)])
     views = views_from_specs(specs)
     plain = [r.render(v, outputs=("rgbd", "hit", "depth", "steps")) for v in views]
-    for launch in [(8, 4, 1, 4, 1), (8, 4, 2, 4, 0), (4, 8, 4, 2, 1), (16, 2, 2, 8, 1)]:
+    for launch in [(8, 4, 1, 4, 1), (8, 4, 2, 4, 0), (4, 8, 4, 2, 1), (16, 2, 2, 8, 1), (8, 4, 1, 6, 1)]:
         r.set_launch(*launch)
         batch = r.render_batch(views, outputs=("rgbd", "hit", "depth", "steps"), device=False)
         for p, b in zip(plain, batch):
@@ -129,12 +130,13 @@ def test_render_batch_equals_plain(scene100k):
         assert np.array_equal(p["hit"], b["hit"])
 
 
-def test_render_independent_of_leaf_size(scene100k):
+def test_render_independent_of_leaf_size_and_search(scene100k):
     sc, _ = scene100k
     v = views_from_specs(syn.make_views(1, seed=4, boxes=sc.boxes, resolutions=[(200, 150)]))[0]
     outs = []
-    for leaf in (8, 16, 32):
-        r, _, _ = make_renderer(sc.xyz, sc.rgb, leaf=leaf)
+    for leaf, search, ctas in ((8, 1, 4), (16, 1, 8), (32, 1, 6), (16, 0, 4)):
+        r, _, _ = make_renderer(sc.xyz, sc.rgb, leaf=leaf, search=search)
+        r.set_launch(search=search, ctas_per_sm=ctas)
         outs.append(r.render(v))
     for o in outs[1:]:
         assert np.array_equal(o["hit"], outs[0]["hit"])
