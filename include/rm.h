@@ -91,6 +91,9 @@ typedef struct {
   int64_t packet_steps;  /* steps answered by a warp packet traversal */
   int64_t solo_steps;    /* steps answered by a per-ray tree walk */
   int64_t packet_leaves; /* leaves scanned by packet traversals */
+  int64_t packet_nodes;  /* tree nodes expanded by packet traversals */
+  int64_t warp_steps;    /* warp-wide distance steps */
+  int64_t split_steps;   /* warp steps whose lanes were split into two packets */
   float kernel_ms;       /* device time of the last render launch (graph for the batch) */
 } rm_stats;
 

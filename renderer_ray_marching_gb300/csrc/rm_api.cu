@@ -572,6 +572,9 @@ rm_status rm_get_stats(rm_ctx* ctx, rm_stats* stats) {
     c.stats.packet_steps = (int64_t)h[4];
     c.stats.solo_steps = (int64_t)h[5];
     c.stats.packet_leaves = (int64_t)h[6];
+    c.stats.packet_nodes = (int64_t)h[7];
+    c.stats.warp_steps = (int64_t)h[8];
+    c.stats.split_steps = (int64_t)h[9];
     c.stats.kernel_ms = ms;
     *stats = c.stats;
     return RM_OK;

@@ -368,7 +368,7 @@ __device__ __forceinline__ void list_consider_unique(KList<K>& L, float d, int32
 // if the stack bound was hit (cannot happen for depth <= MAX_LEVELS).
 template <class List>
 __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, float qz, List& L,
-                           PacketStack& ps, unsigned& leaves) {
+                           PacketStack& ps, unsigned& leaves, unsigned& nodes) {
   const unsigned FULL = 0xffffffffu;
   const float INF = __int_as_float(0x7f800000);
   const int lane = threadIdx.x & 31;
@@ -379,6 +379,7 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   int lvl = 0;
   uint32_t j = 0;
   while (true) {
+    ++nodes;
     const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
     float m0, m1, m2, m3;
     {

@@ -90,10 +90,18 @@ struct ViewArgs {
 };
 
 // counters: [0] steps, [1] rays, [2] hits, [3] search errors,
-//           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets
+//           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets,
+//           [7] nodes expanded by packets, [8] warp steps, [9] warp steps split in two packets
 struct LaneCounters {
-  unsigned steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0;
+  unsigned steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0, nodes = 0,
+           wsteps = 0, split = 0;
 };
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
 
 __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs& v, int64_t pix, int32_t s,
                                              float depth, int32_t steps) {
@@ -163,7 +171,23 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
     float pz = __fmaf_rn(r.dz, t, r.oz);
     if (stepping) L.rewarm(ix, px, py, pz);
     if (SEARCH == 1) {
-      if (!packet_knn(ix, stepping, px, py, pz, L, sm, cnt.leaves)) cnt.bad += stepping ? 1 : 0;
+      // Two packets at most: lanes whose bound is within 4x (in radius) of the
+      // tightest lane's, then the rest (rays just started or still far from
+      // every surface).  One loose lane would otherwise make the whole warp
+      // walk everything inside its ball.
+      float bmin = warp_min(stepping ? L.wd : INFINITY);
+      bool tight = stepping && L.wd <= 16.0f * bmin;
+      unsigned lv = 0, nd = 0;
+      if (!packet_knn(ix, tight, px, py, pz, L, sm, lv, nd)) cnt.bad += tight ? 1 : 0;
+      bool rest = stepping && !tight;
+      if (__ballot_sync(FULL, rest)) {
+        if (!packet_knn(ix, rest, px, py, pz, L, sm, lv, nd)) cnt.bad += rest ? 1 : 0;
+        cnt.split += lane == 0 ? 1 : 0;
+      }
+      cnt.leaves += lane == 0 ? lv : 0;
+      cnt.nodes += lane == 0 ? nd : 0;
+      const unsigned any_step = __ballot_sync(FULL, stepping);  // every lane votes
+      cnt.wsteps += (lane == 0 && any_step) ? 1 : 0;
     } else if (stepping) {
       if (!knn_search(ix, px, py, pz, L)) cnt.bad += 1;
     }
@@ -196,15 +220,15 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
 }
 
 __device__ __forceinline__ void flush_counters(LaneCounters& c, unsigned long long* counters) {
-  unsigned long long v[7] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.leaves};  // widened
+  unsigned long long v[10] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.leaves, c.nodes, c.wsteps, c.split};
 #pragma unroll
-  for (int k = 0; k < 7; ++k) {
+  for (int k = 0; k < 10; ++k) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
   }
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-    for (int k = 0; k < 7; ++k)
+    for (int k = 0; k < 10; ++k)
       if (v[k]) atomicAdd(counters + k, v[k]);
   }
 }

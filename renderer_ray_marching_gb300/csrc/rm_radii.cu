@@ -41,7 +41,7 @@ k_radii_packet(IndexDev ix, float max_radius, float* __restrict__ radii_out, int
   __shared__ PacketStack stacks[RADII_WARPS];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t nwarps = (int64_t)gridDim.x * RADII_WARPS;
-  unsigned leaves = 0;
+  unsigned leaves = 0, nodes = 0;
   for (int64_t wbase = ((int64_t)blockIdx.x * RADII_WARPS + warp) * 32; wbase < ix.n; wbase += nwarps * 32) {
     const int64_t s = wbase + lane;
     const bool active = s < ix.n;
@@ -56,7 +56,7 @@ k_radii_packet(IndexDev ix, float max_radius, float* __restrict__ radii_out, int
         klist_insert<2>(L, d2_point(c, q.x, q.y, q.z), (int32_t)nb, c.w, ix.perm);
       }
     }
-    if (!packet_knn(ix, active, q.x, q.y, q.z, L, stacks[warp], leaves) && active) atomicAdd(err, 1ull);
+    if (!packet_knn(ix, active, q.x, q.y, q.z, L, stacks[warp], leaves, nodes) && active) atomicAdd(err, 1ull);
     if (active) {
       float r = __fsqrt_rn(L.d[1]);
       int32_t i = __ldg(ix.perm + s);
