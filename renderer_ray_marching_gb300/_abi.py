@@ -47,7 +47,8 @@ class RmStats(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_int64), ("steps", ctypes.c_int64), ("hits", ctypes.c_int64),
                 ("packet_steps", ctypes.c_int64), ("solo_steps", ctypes.c_int64),
                 ("packet_leaves", ctypes.c_int64), ("packet_nodes", ctypes.c_int64),
-                ("warp_steps", ctypes.c_int64), ("split_steps", ctypes.c_int64), ("kernel_ms", ctypes.c_float)]
+                ("warp_steps", ctypes.c_int64), ("split_steps", ctypes.c_int64),
+                ("search_errors", ctypes.c_int64), ("kernel_ms", ctypes.c_float)]
 
 
 class RmLaunch(ctypes.Structure):

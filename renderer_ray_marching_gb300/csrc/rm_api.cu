@@ -24,6 +24,10 @@ rm_status fail(Ctx& c, rm_status s, const std::string& msg) {
   return s;
 }
 
+struct KernelError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
 template <class F>
 rm_status guarded(rm_ctx* ctx, F&& f) {
   if (!ctx) return RM_ERR_INVALID;
@@ -32,6 +36,9 @@ rm_status guarded(rm_ctx* ctx, F&& f) {
     if (c.cfg.device >= 0) CK(cudaSetDevice(c.cfg.device));
     c.err.clear();
     return f(c);
+  } catch (const KernelError& e) {
+    c.err = e.what();
+    return RM_ERR_KERNEL;
   } catch (const OomError& e) {
     c.err = e.what();
     return RM_ERR_OOM;
@@ -67,11 +74,15 @@ const void* stage_in(Ctx& c, DevBuf& buf, const void* src, size_t bytes, int loc
   return buf.p;
 }
 
+// Error slots: the radii/kNN kernels count failed searches at err_counter,
+// the marchers at counters[3] (stack bound or node budget exceeded).
 void check_kernel_errors(Ctx& c) {
-  unsigned long long e = 0;
-  CK(cudaMemcpyAsync(&e, err_counter(c), sizeof(e), cudaMemcpyDeviceToHost, c.stream));
+  unsigned long long e[2] = {0, 0};
+  CK(cudaMemcpyAsync(&e[0], err_counter(c), sizeof(e[0]), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(&e[1], counters(c) + 3, sizeof(e[1]), cudaMemcpyDeviceToHost, c.stream));
   CK(cudaStreamSynchronize(c.stream));
-  if (e) throw std::runtime_error("kernel reported " + std::to_string(e) + " search-stack overflows");
+  if (e[0] || e[1])
+    throw KernelError("kernel reported " + std::to_string(e[0] + e[1]) + " incomplete nearest-neighbour searches");
 }
 
 bool view_ok(const rm_view& v, std::string* why) {
@@ -575,6 +586,7 @@ rm_status rm_get_stats(rm_ctx* ctx, rm_stats* stats) {
     c.stats.packet_nodes = (int64_t)h[7];
     c.stats.warp_steps = (int64_t)h[8];
     c.stats.split_steps = (int64_t)h[9];
+    c.stats.search_errors = (int64_t)h[3];
     c.stats.kernel_ms = ms;
     *stats = c.stats;
     return RM_OK;

@@ -330,6 +330,9 @@ __device__ bool knn_search(const IndexDev& ix, float qx, float qy, float qz, Lis
 // Per-warp shared memory of a packet traversal: pending nodes (their boxes
 // are re-read from the parent's group and re-tested when popped).
 constexpr int PSTACK = 3 * MAX_LEVELS + 4;
+// Node expansions one packet walk may take before it gives up and reports
+// an error (far above any exact search's need; only a broken bound hits it).
+constexpr unsigned PACKET_NODE_BUDGET = 1u << 20;
 struct PacketStack {
   uint32_t code[PSTACK];
 };
@@ -378,8 +381,10 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   int sp = 0;
   int lvl = 0;
   uint32_t j = 0;
+  unsigned budget = PACKET_NODE_BUDGET;
   while (true) {
     ++nodes;
+    if (--budget == 0) return false;  // self-check: a walk this long means a broken bound
     const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
     float m0, m1, m2, m3;
     {
@@ -390,9 +395,10 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
       m2 = active ? d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz) : INF;
       m3 = active ? d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz) : INF;
     }
+    // only active lanes vote: an idle lane's bound may be +inf, and inf <= inf
     const float w = list_worst(L);
-    const unsigned n0 = __ballot_sync(FULL, m0 <= w), n1 = __ballot_sync(FULL, m1 <= w);
-    const unsigned n2 = __ballot_sync(FULL, m2 <= w), n3 = __ballot_sync(FULL, m3 <= w);
+    const unsigned n0 = __ballot_sync(FULL, active && m0 <= w), n1 = __ballot_sync(FULL, active && m1 <= w);
+    const unsigned n2 = __ballot_sync(FULL, active && m2 <= w), n3 = __ballot_sync(FULL, active && m3 <= w);
     float k0 = __shfl_sync(FULL, m0, leader), k1 = __shfl_sync(FULL, m1, leader);
     float k2 = __shfl_sync(FULL, m2, leader), k3 = __shfl_sync(FULL, m3, leader);
     int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
@@ -411,7 +417,7 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
         if (!(needm & (1u << c))) continue;
         // bounds may have shrunk while scanning nearer leaves
         const float mc = c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3;
-        if (!__ballot_sync(FULL, mc <= list_worst(L))) continue;
+        if (!__ballot_sync(FULL, active && mc <= list_worst(L))) continue;
         int64_t start = (int64_t)(base + c) * ix.leaf;
         int64_t end = start + ix.leaf;
         if (end > ix.n) end = ix.n;
@@ -463,7 +469,7 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
       if (active)
         md = d2_box(__ldg(pg + 0 + c), __ldg(pg + 4 + c), __ldg(pg + 8 + c), __ldg(pg + 12 + c),
                     __ldg(pg + 16 + c), __ldg(pg + 20 + c), qx, qy, qz);
-      if (__ballot_sync(FULL, md <= list_worst(L))) {
+      if (__ballot_sync(FULL, active && md <= list_worst(L))) {
         lvl = plvl;
         j = pj;
         found = true;

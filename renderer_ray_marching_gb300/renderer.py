@@ -273,6 +273,7 @@ class Renderer:
         s = _abi.RmStats()
         self._check(self._lib.rm_get_stats(self._h, ctypes.byref(s)))
         return {"rays": s.rays, "steps": s.steps, "hits": s.hits, "packet_steps": s.packet_steps,
+                "search_errors": s.search_errors,
                 "solo_steps": s.solo_steps, "packet_leaves": s.packet_leaves, "packet_nodes": s.packet_nodes,
                 "warp_steps": s.warp_steps, "split_steps": s.split_steps, "kernel_ms": s.kernel_ms}
 

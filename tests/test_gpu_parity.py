@@ -109,6 +109,11 @@ def test_render_plain_matches_oracle(scene100k):
     assert np.array_equal(rgbd[m, :3], col)
     assert np.array_equal(rgbd[m, 3], out["depth"].reshape(-1)[m])
     assert np.all(rgbd[~m] == 0)
+    # work bound: a packet never walks the whole tree (border tiles hold idle
+    # lanes whose bound is +inf; they must not vote)
+    st = r.stats()
+    assert st["search_errors"] == 0
+    assert st["packet_nodes"] / max(st["warp_steps"], 1) < 100, st
 
 
 def test_render_batch_equals_plain(scene100k):
