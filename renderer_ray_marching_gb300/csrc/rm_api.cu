@@ -686,26 +686,25 @@ rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* c
       }
       return best;
     };
+    // Packet search keeps a tile's rays in lockstep (refilling lanes mid-tile
+    // breaks the coherence it lives on), so rays_per_lane > 1 is tried with
+    // the per-ray walk only.
     const int shapes[3][2] = {{8, 4}, {4, 8}, {16, 2}};
-    const int rpls[3] = {1, 2, 4};
     rm_launch best_l = c.launch;
     float best_t = 1e30f;
-    for (auto& sh : shapes)
-      for (int rpl : rpls) {
-        rm_launch L{sh[0], sh[1], rpl, 4, best_l.search};
-        float t = time_once(L);
-        if (t < best_t) { best_t = t; best_l = L; }
-      }
-    for (int mode : {0, 1}) {
-      if (mode == best_l.search) continue;
-      rm_launch L = best_l;
-      L.search = mode;
+    for (auto& sh : shapes) {
+      rm_launch L{sh[0], sh[1], 1, 4, 1};
       float t = time_once(L);
       if (t < best_t) { best_t = t; best_l = L; }
     }
-    for (int ctas : {2, 6, 8}) {
+    for (int ctas : {6, 8}) {
       rm_launch L = best_l;
       L.ctas_per_sm = ctas;
+      float t = time_once(L);
+      if (t < best_t) { best_t = t; best_l = L; }
+    }
+    for (int rpl : {1, 2}) {
+      rm_launch L{best_l.tile_w, best_l.tile_h, rpl, 4, 0};
       float t = time_once(L);
       if (t < best_t) { best_t = t; best_l = L; }
     }

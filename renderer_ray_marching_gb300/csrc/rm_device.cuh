@@ -335,6 +335,7 @@ constexpr int PSTACK = 3 * MAX_LEVELS + 4;
 constexpr unsigned PACKET_NODE_BUDGET = 1u << 20;
 struct PacketStack {
   uint32_t code[PSTACK];
+  float4 rec[32];  // one staged leaf (leaf size <= 32)
 };
 
 __device__ __forceinline__ void list_consider_unique(KSet& L, float d, int32_t s, float r,
@@ -395,38 +396,48 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
       m2 = active ? d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz) : INF;
       m3 = active ? d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz) : INF;
     }
-    // only active lanes vote: an idle lane's bound may be +inf, and inf <= inf
+    // needed children: one OR-reduction of every active lane's 4-bit vote
+    // (idle lanes do not vote: their bound may be +inf, and inf <= inf)
     const float w = list_worst(L);
-    const unsigned n0 = __ballot_sync(FULL, active && m0 <= w), n1 = __ballot_sync(FULL, active && m1 <= w);
-    const unsigned n2 = __ballot_sync(FULL, active && m2 <= w), n3 = __ballot_sync(FULL, active && m3 <= w);
-    float k0 = __shfl_sync(FULL, m0, leader), k1 = __shfl_sync(FULL, m1, leader);
-    float k2 = __shfl_sync(FULL, m2, leader), k3 = __shfl_sync(FULL, m3, leader);
-    int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
-    RM_CSWAP_U(k0, o0, k1, o1);
-    RM_CSWAP_U(k2, o2, k3, o3);
-    RM_CSWAP_U(k0, o0, k2, o2);
-    RM_CSWAP_U(k1, o1, k3, o3);
-    RM_CSWAP_U(k1, o1, k2, o2);
-    // 4-bit mask of the needed children (warp-uniform)
-    const unsigned needm = (n0 ? 1u : 0u) | (n1 ? 2u : 0u) | (n2 ? 4u : 0u) | (n3 ? 8u : 0u);
+    unsigned mine = 0;
+    if (active) mine = (m0 <= w ? 1u : 0u) | (m1 <= w ? 2u : 0u) | (m2 <= w ? 4u : 0u) | (m3 <= w ? 8u : 0u);
+    const unsigned needm = __reduce_or_sync(FULL, mine);
+    // visiting order: nearest first for the leading lane, sent as one packed byte
+    unsigned order;
+    {
+      float k0 = m0, k1 = m1, k2 = m2, k3 = m3;
+      int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
+      RM_CSWAP_U(k0, o0, k1, o1);
+      RM_CSWAP_U(k2, o2, k3, o3);
+      RM_CSWAP_U(k0, o0, k2, o2);
+      RM_CSWAP_U(k1, o1, k3, o3);
+      RM_CSWAP_U(k1, o1, k2, o2);
+      order = (unsigned)o0 | ((unsigned)o1 << 2) | ((unsigned)o2 << 4) | ((unsigned)o3 << 6);
+    }
+    order = __shfl_sync(FULL, order, leader);
     const uint32_t base = j * 4u;
     if (lvl + 1 == ix.depth) {
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
+        const int c = (int)((order >> (2 * t)) & 3u);
         if (!(needm & (1u << c))) continue;
         // bounds may have shrunk while scanning nearer leaves
         const float mc = c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3;
         if (!__ballot_sync(FULL, active && mc <= list_worst(L))) continue;
-        int64_t start = (int64_t)(base + c) * ix.leaf;
-        int64_t end = start + ix.leaf;
-        if (end > ix.n) end = ix.n;
+        const int64_t start = (int64_t)(base + c) * ix.leaf;
+        const int cnt = (int)min((int64_t)ix.leaf, ix.n - start);
         ++leaves;
-        for (int64_t i = start; i < end; ++i) {
-          float4 cr = __ldg(ix.rec + i);
-          if (active) {
+        // one coalesced load of the leaf into shared memory, then broadcast reads
+        __syncwarp();
+        if (lane < cnt) {
+          ps.rec[lane] = __ldg(ix.rec + start + lane);
+        }
+        __syncwarp();
+        if (active) {
+          for (int k = 0; k < cnt; ++k) {
+            float4 cr = ps.rec[k];
             float d = d2_point(cr, qx, qy, qz);
-            if (d <= list_worst(L)) list_consider_unique(L, d, (int32_t)i, cr.w, ix.perm);
+            if (d <= list_worst(L)) list_consider_unique(L, d, (int32_t)(start + k), cr.w, ix.perm);
           }
         }
       }
@@ -435,14 +446,14 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
       int first = -1;
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
+        const int c = (int)((order >> (2 * t)) & 3u);
         if ((needm & (1u << c)) && first < 0) first = c;
       }
       if (sp + 3 > PSTACK) return false;
       const uint32_t code = (uint32_t)(lvl + 1) << 28;
 #pragma unroll
       for (int t = 3; t >= 0; --t) {
-        const int c = t == 0 ? o0 : t == 1 ? o1 : t == 2 ? o2 : o3;
+        const int c = (int)((order >> (2 * t)) & 3u);
         if ((needm & (1u << c)) && c != first) {
           if (lane == 0) ps.code[sp] = code | (base + c);
           ++sp;
