@@ -434,19 +434,7 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
         }
         __syncwarp();
         if (active) {
-          // pass 1 (no divergence): which staged points are within this lane's bound
-          const float w0 = list_worst(L);
-          unsigned mask = 0;
-#pragma unroll 4
           for (int k = 0; k < cnt; ++k) {
-            float d = d2_point(ps.rec[k], qx, qy, qz);
-            mask |= (d <= w0 ? 1u : 0u) << k;
-          }
-          // pass 2: insert this lane's candidates only (the bound only shrinks,
-          // so re-testing against it keeps the set exact)
-          while (mask) {
-            const int k = __ffs(mask) - 1;
-            mask &= mask - 1u;
             float4 cr = ps.rec[k];
             float d = d2_point(cr, qx, qy, qz);
             if (d <= list_worst(L)) list_consider_unique(L, d, (int32_t)(start + k), cr.w, ix.perm);
