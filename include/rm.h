@@ -194,6 +194,26 @@ rm_status rm_backward(rm_ctx* ctx, const rm_view* views, int32_t n, const float*
 /* Number of points in the context's cloud. */
 int64_t rm_cloud_size(const rm_ctx* ctx);
 
+/* Allocation-free batched form (no counterpart in the reference).  For
+ * callers that cannot allocate device memory: an application whose GPU
+ * memory is all handed out by its own pool, a process under a fixed device
+ * memory cap, or a loop that cannot afford the device-wide synchronisation
+ * of cudaMalloc/cudaFree.  Renders like rm_render_batch into DEVICE outputs
+ * (every non-NULL rm_frame pointer is a device pointer), but allocates
+ * nothing and uses no CUDA graph: its scratch (work queue, counters and a
+ * view table) is one static device array of RM_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading the library holds until exit.  At most
+ * RM_NOALLOC_MAX_VIEWS views per call (more returns RM_ERR_LIMIT); the cloud
+ * must be non-empty.  The first call on a device looks up the array's device
+ * address; make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race, so serialise them.  Returns after the
+ * frames are written (it synchronises the context's stream).  rm_get_stats
+ * does not count its work. */
+#define RM_NOALLOC_MAX_VIEWS 1024
+#define RM_NOALLOC_SCRATCH_BYTES (256 + 1024 * 136)
+rm_status rm_render_batch_noalloc(rm_ctx* ctx, const rm_view* views, int32_t n,
+                                  const rm_frame* out);
+
 #ifdef __cplusplus
 }
 #endif

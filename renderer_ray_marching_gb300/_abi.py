@@ -23,7 +23,7 @@ EXPORTS = [
     "rm_config_default", "rm_ctx_create", "rm_ctx_destroy", "rm_last_error", "rm_synchronize",
     "rm_cloud_set", "rm_index_build", "rm_knn", "rm_radii_compute", "rm_radii_set",
     "rm_view_pane", "rm_render", "rm_render_batch", "rm_set_launch", "rm_get_launch",
-    "rm_autotune", "rm_get_stats", "rm_backward", "rm_cloud_size",
+    "rm_autotune", "rm_get_stats", "rm_backward", "rm_cloud_size", "rm_render_batch_noalloc",
 ]
 
 
@@ -102,6 +102,7 @@ def load(build_if_missing: bool = True):
             "rm_get_stats": (I32, [P, P]),
             "rm_backward": (I32, [P, P, I32, P, P, P, P, P, P, I32]),
             "rm_cloud_size": (I64, [P]),
+            "rm_render_batch_noalloc": (I32, [P, P, I32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

@@ -25,7 +25,8 @@ LIB = os.path.join(LIBDIR, "librm_gb300.so")
 CLI = os.path.join(LIBDIR, "marcher.bin")
 IOLIB = os.path.join(LIBDIR, "librm_io.so")
 
-CUDA_SOURCES = ["rm_index.cu", "rm_radii.cu", "rm_march.cu", "rm_backward.cu", "rm_api.cu"]
+CUDA_SOURCES = ["rm_index.cu", "rm_radii.cu", "rm_march.cu", "rm_backward.cu", "rm_api.cu",
+                "rm_noalloc.cu"]
 HOST_SOURCES = ["marcher_main.cpp", "io.cpp", "rmio_c.cpp"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]

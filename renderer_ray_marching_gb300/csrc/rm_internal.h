@@ -155,6 +155,9 @@ void launch_render_plain(Ctx& c, const rm_view& v, float4* rgbd, int32_t* hit, f
 void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_tiles,
                          const rm_launch& L, unsigned long long* counters);
 void launch_prepare_views(Ctx& c, ViewDev* views_dev, int n, unsigned long long* counters);
+void launch_render_batch_queue(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
+                               const rm_launch& L, unsigned long long* queue,
+                               unsigned long long* counters);
 
 // rm_backward.cu
 void launch_backward(Ctx& c, const ViewDev* views_dev, int n, int64_t total_pixels,

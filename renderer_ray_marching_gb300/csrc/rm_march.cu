@@ -415,4 +415,31 @@ void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
   }
 }
 
+// Same launch as launch_render_batch with a caller-supplied queue counter
+// (used by the allocation-free entry point, whose scratch is static).
+void launch_render_batch_queue(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
+                               const rm_launch& L, unsigned long long* queue,
+                               unsigned long long* counters) {
+  BatchArgs a;
+  a.views = views_dev;
+  a.nviews = n;
+  a.total_items = total_items;
+  a.tile_w = L.tile_w;
+  a.tile_h = L.tile_h;
+  a.rpl = L.rays_per_lane;
+  int grid = c.sm_count * (L.ctas_per_sm > 0 ? L.ctas_per_sm : 4);
+  MarchParams mp = march_params(c);
+  auto go = [&](auto kern) {
+    kern<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, mp, queue, counters);
+  };
+  const int cps = L.ctas_per_sm;
+  if (mp.search == 1) {
+    if (cps >= 8) go(k_march_batch<1, 8>);
+    else if (cps >= 6) go(k_march_batch<1, 6>);
+    else go(k_march_batch<1, 4>);
+  } else {
+    go(k_march_batch<0, 4>);
+  }
+}
+
 }  // namespace rm
