@@ -112,20 +112,23 @@ __device__ __forceinline__ float klist_worst(const KList<K>& L) {
   return L.d[K - 1];
 }
 
-// The marcher's 10 nearest, kept as an unsorted set with its worst entry
-// (largest (d2, cloud index)) tracked: an insertion replaces the worst slot
-// and the new worst comes from a 4-level reduction tree; re-seeding at the
-// next step's position re-measures the ten points without sorting.
+// The marcher's 10 nearest, kept sorted by (d2, cloud index) in registers
+// (empty slots (+inf, -1) last), so the bound is always d[KNN-1].
 // Insertions skip points already present, so the set can start from the
 // previous step's points (they are valid candidates: the search then prunes
 // with a finite bound from the first node and stays exact).  Radii are not
 // kept here; the step value reads them from the records.
+//
+// Cost.  An insertion is the hot divergent path of the packet walk (about
+// 80 per ray step at 20M points), so its common case touches no memory and
+// takes no branch: one equality scan over the distances, then one
+// compare-and-select pass that slides the new entry into place.  A
+// duplicate of a present point has the same record and query, hence the
+// same d2 bits, so the equality scan catches duplicates together with exact
+// distance ties; both go to the ordered path that compares cloud indices.
 struct KSet {
   float d[KNN];
   int32_t s[KNN];   // sorted position, -1 = empty
-  float wd;         // worst entry: d2, position, slot
-  int32_t ws;
-  int wi;
 
   __device__ __forceinline__ void clear() {
 #pragma unroll
@@ -133,73 +136,101 @@ struct KSet {
       d[j] = __int_as_float(0x7f800000);
       s[j] = -1;
     }
-    wd = __int_as_float(0x7f800000);
-    ws = -1;
-    wi = 0;
   }
 
-  // (da, sa) after (db, sb) in (d2, cloud index) order; empty slots are last.
-  static __device__ __forceinline__ bool later(float da, int32_t sa, float db, int32_t sb,
-                                               const int32_t* __restrict__ perm) {
-    if (da != db) return da > db;
-    if (sb < 0) return false;
-    if (sa < 0) return true;
-    return __ldg(perm + sa) > __ldg(perm + sb);
-  }
+  __device__ __forceinline__ float worst() const { return d[KNN - 1]; }
 
-  __device__ __forceinline__ void recompute_worst(const int32_t* __restrict__ perm) {
-    float td[KNN / 2];
-    int32_t ts[KNN / 2];
-    int ti[KNN / 2];
-#pragma unroll
-    for (int p = 0; p < KNN / 2; ++p) {
-      bool a = later(d[2 * p], s[2 * p], d[2 * p + 1], s[2 * p + 1], perm);
-      td[p] = a ? d[2 * p] : d[2 * p + 1];
-      ts[p] = a ? s[2 * p] : s[2 * p + 1];
-      ti[p] = a ? 2 * p : 2 * p + 1;
-    }
-    // 5 -> 2 (+1) -> 1
-    bool a01 = later(td[0], ts[0], td[1], ts[1], perm);
-    float d01 = a01 ? td[0] : td[1];
-    int32_t s01 = a01 ? ts[0] : ts[1];
-    int i01 = a01 ? ti[0] : ti[1];
-    bool a23 = later(td[2], ts[2], td[3], ts[3], perm);
-    float d23 = a23 ? td[2] : td[3];
-    int32_t s23 = a23 ? ts[2] : ts[3];
-    int i23 = a23 ? ti[2] : ti[3];
-    bool a03 = later(d01, s01, d23, s23, perm);
-    float d03 = a03 ? d01 : d23;
-    int32_t s03 = a03 ? s01 : s23;
-    int i03 = a03 ? i01 : i23;
-    bool a4 = later(d03, s03, td[4], ts[4], perm);
-    wd = a4 ? d03 : td[4];
-    ws = a4 ? s03 : ts[4];
-    wi = a4 ? i03 : ti[4];
-  }
-
-  // Candidate (dd, ss) with dd <= wd.
+  // Candidate (dd, ss) with dd <= worst().
   __device__ __forceinline__ void consider(float dd, int32_t ss, const int32_t* __restrict__ perm) {
-    if (dd == wd && ws >= 0 && !(__ldg(perm + ss) < __ldg(perm + ws))) return;
+    bool eq = false;
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) eq |= (d[j] == dd);
+    if (eq) {
+      consider_ordered(dd, ss, perm);
+      return;
+    }
+    // no entry at distance dd: order by d2 alone
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      const bool sw = d[j] > dd;
+      const float td = d[j];
+      const int32_t ts = s[j];
+      d[j] = sw ? dd : td;
+      s[j] = sw ? ss : ts;
+      dd = sw ? td : dd;
+      ss = sw ? ts : ss;
+    }
+  }
+
+  // Equal distances present: skip a duplicate, else insert by (d2, cloud index).
+  __device__ __forceinline__ void consider_ordered(float dd, int32_t ss, const int32_t* __restrict__ perm) {
     bool dup = false;
 #pragma unroll
     for (int j = 0; j < KNN; ++j) dup |= (s[j] == ss);
     if (dup) return;
 #pragma unroll
     for (int j = 0; j < KNN; ++j) {
-      if (j == wi) {
+      if (s[j] < 0 || knn_before(dd, ss, d[j], s[j], perm)) {  // empty slots are last
+        const float td = d[j];
+        const int32_t ts = s[j];
         d[j] = dd;
         s[j] = ss;
+        dd = td;
+        ss = ts;
       }
     }
-    recompute_worst(perm);
   }
 
+  // (d, s) pairs a and b in order (a first) by d2; equal d2 is left for the
+  // tie pass below.
+  __device__ __forceinline__ void cas(int a, int b) {
+    const bool sw = d[b] < d[a];
+    const float da = d[a], db = d[b];
+    const int32_t sa = s[a], sb = s[b];
+    d[a] = sw ? db : da;
+    d[b] = sw ? da : db;
+    s[a] = sw ? sb : sa;
+    s[b] = sw ? sa : sb;
+  }
+
+  // Re-measure the ten points at the next step's position and re-sort:
+  // a 29-comparator network on d2, then, only if two finite distances are
+  // equal, an insertion pass by (d2, cloud index).
   __device__ __forceinline__ void rewarm(const IndexDev& ix, float qx, float qy, float qz) {
 #pragma unroll
     for (int j = 0; j < KNN; ++j) {
       if (s[j] >= 0) d[j] = d2_point(__ldg(ix.rec + s[j]), qx, qy, qz);
     }
-    recompute_worst(ix.perm);
+    static_assert(KNN == 10, "sorting network is for 10 entries");
+    cas(4, 9); cas(3, 8); cas(2, 7); cas(1, 6); cas(0, 5);
+    cas(1, 4); cas(6, 9); cas(0, 3); cas(5, 8);
+    cas(0, 2); cas(3, 6); cas(7, 9);
+    cas(0, 1); cas(2, 4); cas(5, 7); cas(8, 9);
+    cas(1, 2); cas(4, 6); cas(7, 8); cas(3, 5);
+    cas(2, 5); cas(6, 8); cas(1, 3); cas(4, 7);
+    cas(2, 3); cas(6, 7);
+    cas(3, 4); cas(5, 6);
+    cas(4, 5);
+    bool tie = false;
+#pragma unroll
+    for (int j = 0; j + 1 < KNN; ++j) tie |= (d[j] == d[j + 1] && s[j + 1] >= 0);
+    if (tie) {
+      // insertion sort by (d2, cloud index); equal-d2 runs are short
+#pragma unroll
+      for (int i = 1; i < KNN; ++i) {
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+          if (s[j] >= 0 && knn_before(d[j], s[j], d[j - 1], s[j - 1], ix.perm)) {
+            const float td = d[j];
+            const int32_t ts = s[j];
+            d[j] = d[j - 1];
+            s[j] = s[j - 1];
+            d[j - 1] = td;
+            s[j - 1] = ts;
+          }
+        }
+      }
+    }
   }
 
   // src/ray_marching.cu:280-290: min of sqrtf(d2) - r visiting candidates
@@ -227,7 +258,7 @@ struct KSet {
   }
 };
 
-__device__ __forceinline__ float list_worst(const KSet& L) { return L.wd; }
+__device__ __forceinline__ float list_worst(const KSet& L) { return L.worst(); }
 template <int K>
 __device__ __forceinline__ float list_worst(const KList<K>& L) { return L.d[K - 1]; }
 __device__ __forceinline__ void list_consider(KSet& L, float d, int32_t s, float r, const int32_t* perm) {

@@ -175,8 +175,8 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
       // tightest lane's, then the rest (rays just started or still far from
       // every surface).  One loose lane would otherwise make the whole warp
       // walk everything inside its ball.
-      float bmin = warp_min(stepping ? L.wd : INFINITY);
-      bool tight = stepping && L.wd <= 16.0f * bmin;
+      float bmin = warp_min(stepping ? L.worst() : INFINITY);
+      bool tight = stepping && L.worst() <= 16.0f * bmin;
       unsigned lv = 0, nd = 0;
       if (!packet_knn(ix, tight, px, py, pz, L, sm, lv, nd)) cnt.bad += tight ? 1 : 0;
       bool rest = stepping && !tight;
