@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--points", type=int, default=20_000_000)
     ap.add_argument("--views", type=int, default=256)
-    ap.add_argument("--cpu-rays", type=int, default=40_000, help="rays per CPU-baseline sample")
+    ap.add_argument("--cpu-rays", type=int, default=2_000_000,
+                    help="rays per CPU-baseline sample (about 12 s of 16-core CPU work at 20M points)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     # switches for short profiling runs (never used for a reported number)
     ap.add_argument("--no-autotune", action="store_true")
@@ -384,6 +385,8 @@ def main():
                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                         "bytes_model": "20 B out + 16 B colour per hit + 160 B per distance step (10 float4 candidates)",
+                        "sm_issue_active_pct": None if tr is None else tr.get("sm_issue_active_pct"),
+                        "l2_hit_pct": None if tr is None else tr.get("l2_hit_pct"),
                         "kernel_ms": round(kms, 3)},
            "clocks": clk,
            "gpu_launches": 2 * args.steps}

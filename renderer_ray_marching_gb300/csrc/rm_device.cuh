@@ -24,7 +24,7 @@ constexpr float ZFAR = 100.0f;      // src/common.h:4
 constexpr float ZNEAR = 0.1f;       // src/common.h:5
 constexpr int MAX_STEPS = 128;      // src/common.h:6
 constexpr float MIN_DIST = 0.001f;  // src/common.h:7
-constexpr int MAX_LEVELS = 14;      // 4^14 leaf slots
+constexpr int MAX_LEVELS = 14;      // 4^14 leaf slots (group offsets stay 32-bit)
 constexpr int STACK = 3 * MAX_LEVELS + 4;
 constexpr int GROUP_F4 = 8;         // float4 per child group (6 used)
 
@@ -39,9 +39,12 @@ struct IndexDev {
   int32_t depth;         // level of the leaves (>= 1); the root is level 0
 };
 
-// Offset of the first child group of level `lvl` (levels 0..depth-1 own groups).
+// Offset of the first child group of level `lvl` (levels 0..depth-1 own
+// groups).  32-bit arithmetic: (4^lvl - 1) / 3 fits for lvl <= MAX_LEVELS,
+// and a 32-bit division by a constant is a multiply-high where the 64-bit
+// one is a multi-instruction sequence on the walk's per-node path.
 __host__ __device__ __forceinline__ int64_t group_offset(int lvl) {
-  return (int64_t)(((1ull << (2 * lvl)) - 1ull) / 3ull);
+  return (int64_t)(((1u << (2 * lvl)) - 1u) / 3u);
 }
 
 __device__ __forceinline__ float d2_point(float4 c, float qx, float qy, float qz) {
@@ -409,7 +412,11 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   const int lane = threadIdx.x & 31;
   unsigned act = __ballot_sync(FULL, active);
   if (act == 0 || ix.n <= 0) return true;
-  const int leader = __ffs(act) - 1;
+  // the visiting order follows one lane: a central pixel of an 8x4 tile
+  // (lanes 11, 12, 19, 20) when one is active, whose nearest-first order
+  // suits its neighbours better than a corner's
+  const unsigned central = act & 0x00181800u;
+  const int leader = __ffs(central ? central : act) - 1;
   int sp = 0;
   int lvl = 0;
   uint32_t j = 0;

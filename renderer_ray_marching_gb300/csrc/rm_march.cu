@@ -171,12 +171,12 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
     float pz = __fmaf_rn(r.dz, t, r.oz);
     if (stepping) L.rewarm(ix, px, py, pz);
     if (SEARCH == 1) {
-      // Two packets at most: lanes whose bound is within 4x (in radius) of the
+      // Two packets at most: lanes whose bound is within 8x (in radius; 64x in d2) of the
       // tightest lane's, then the rest (rays just started or still far from
       // every surface).  One loose lane would otherwise make the whole warp
       // walk everything inside its ball.
       float bmin = warp_min(stepping ? L.worst() : INFINITY);
-      bool tight = stepping && L.worst() <= 16.0f * bmin;
+      bool tight = stepping && L.worst() <= 64.0f * bmin;
       unsigned lv = 0, nd = 0;
       if (!packet_knn(ix, tight, px, py, pz, L, sm, lv, nd)) cnt.bad += tight ? 1 : 0;
       bool rest = stepping && !tight;
