@@ -396,14 +396,21 @@ __device__ __forceinline__ void list_consider_unique(KList<K>& L, float d, int32
 
 // Warp packet traversal: exact k-NN of every active lane's query with one
 // walk of the tree for the whole warp.  A node is expanded when its box lies
-// within the current k-th distance of ANY active lane (one __ballot_sync per
-// child), children are visited nearest-first for the leading lane, pending
-// nodes wait on a shared-memory stack with their boxes and are re-tested
-// when popped, and a leaf's records are read once for the warp (broadcast
-// loads) while every lane updates its own list.  Lists may arrive seeded
-// (insertions skip points already present).  All 32 lanes call it with
-// warp-uniform control flow; inactive lanes only follow along.  Returns false
-// if the stack bound was hit (cannot happen for depth <= MAX_LEVELS).
+// within the current k-th distance of ANY active lane (one OR-reduction of
+// 4-bit votes per node), children are visited nearest-first for the leading
+// lane, pending nodes wait on a shared-memory stack and are re-tested when
+// popped (their boxes re-read from the parent's group), and a leaf's records
+// are staged once for the warp (broadcast loads) while every lane updates
+// its own list.  Lists may arrive seeded (insertions skip points already
+// present).  All 32 lanes call it with warp-uniform control flow; inactive
+// lanes only follow along.  Returns false if the stack bound or the node
+// budget was hit (neither can happen for depth <= MAX_LEVELS and an exact
+// bound).
+//
+// Nodes are addressed by their group's level-order index G: the children of
+// G have groups 4G + 1 + c, and a stack entry holds (level << 28) | G, so no
+// level offset is computed on the walk.  Leaves are never pushed: they are
+// scanned in order when their parent (a node of level depth-1) is expanded.
 template <class List>
 __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, float qz, List& L,
                            PacketStack& ps, unsigned& leaves, unsigned& nodes) {
@@ -417,22 +424,23 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   // suits its neighbours better than a corner's
   const unsigned central = act & 0x00181800u;
   const int leader = __ffs(central ? central : act) - 1;
+  const uint32_t last_first = (uint32_t)group_offset(ix.depth - 1);  // first group of level depth-1
   int sp = 0;
   int lvl = 0;
-  uint32_t j = 0;
+  uint32_t G = 0;
   unsigned budget = PACKET_NODE_BUDGET;
   while (true) {
     ++nodes;
     if (--budget == 0) return false;  // self-check: a walk this long means a broken bound
-    const float4* g = ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(lvl) + j);
+    const float4* g = ix.groups + (size_t)GROUP_F4 * G;
     float m0, m1, m2, m3;
     {
       float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
       float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
-      m0 = active ? d2_box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, qx, qy, qz) : INF;
-      m1 = active ? d2_box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, qx, qy, qz) : INF;
-      m2 = active ? d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz) : INF;
-      m3 = active ? d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz) : INF;
+      m0 = d2_box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, qx, qy, qz);
+      m1 = d2_box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, qx, qy, qz);
+      m2 = d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz);
+      m3 = d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz);
     }
     // needed children: one OR-reduction of every active lane's 4-bit vote
     // (idle lanes do not vote: their bound may be +inf, and inf <= inf)
@@ -440,67 +448,66 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
     unsigned mine = 0;
     if (active) mine = (m0 <= w ? 1u : 0u) | (m1 <= w ? 2u : 0u) | (m2 <= w ? 4u : 0u) | (m3 <= w ? 8u : 0u);
     const unsigned needm = __reduce_or_sync(FULL, mine);
-    // visiting order: nearest first for the leading lane, sent as one packed byte
-    unsigned order;
-    {
-      float k0 = m0, k1 = m1, k2 = m2, k3 = m3;
-      int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
-      RM_CSWAP_U(k0, o0, k1, o1);
-      RM_CSWAP_U(k2, o2, k3, o3);
-      RM_CSWAP_U(k0, o0, k2, o2);
-      RM_CSWAP_U(k1, o1, k3, o3);
-      RM_CSWAP_U(k1, o1, k2, o2);
-      order = (unsigned)o0 | ((unsigned)o1 << 2) | ((unsigned)o2 << 4) | ((unsigned)o3 << 6);
-    }
-    order = __shfl_sync(FULL, order, leader);
-    const uint32_t base = j * 4u;
-    if (lvl + 1 == ix.depth) {
+    if (needm != 0) {
+      // visiting order (2 bits per position, nearest first for the leading
+      // lane); with one needed child any order will do
+      unsigned order = 0xE4u;  // 0, 1, 2, 3
+      if (needm & (needm - 1u)) {
+        float k0 = m0, k1 = m1, k2 = m2, k3 = m3;
+        int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
+        RM_CSWAP_U(k0, o0, k1, o1);
+        RM_CSWAP_U(k2, o2, k3, o3);
+        RM_CSWAP_U(k0, o0, k2, o2);
+        RM_CSWAP_U(k1, o1, k3, o3);
+        RM_CSWAP_U(k1, o1, k2, o2);
+        order = __shfl_sync(FULL, (unsigned)o0 | ((unsigned)o1 << 2) | ((unsigned)o2 << 4) | ((unsigned)o3 << 6),
+                            leader);
+      }
+      if (lvl + 1 == ix.depth) {
+        const uint32_t lbase = (G - last_first) * 4u;
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int c = (int)((order >> (2 * t)) & 3u);
-        if (!(needm & (1u << c))) continue;
-        // bounds may have shrunk while scanning nearer leaves
-        const float mc = c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3;
-        if (!__ballot_sync(FULL, active && mc <= list_worst(L))) continue;
-        const int64_t start = (int64_t)(base + c) * ix.leaf;
-        const int cnt = (int)min((int64_t)ix.leaf, ix.n - start);
-        ++leaves;
-        // one coalesced load of the leaf into shared memory, then broadcast reads
-        __syncwarp();
-        if (lane < cnt) {
-          ps.rec[lane] = __ldg(ix.rec + start + lane);
-        }
-        __syncwarp();
-        if (active) {
-          for (int k = 0; k < cnt; ++k) {
-            float4 cr = ps.rec[k];
-            float d = d2_point(cr, qx, qy, qz);
-            if (d <= list_worst(L)) list_consider_unique(L, d, (int32_t)(start + k), cr.w, ix.perm);
+        for (int t = 0; t < 4; ++t) {
+          const int c = (int)((order >> (2 * t)) & 3u);
+          if (!(needm & (1u << c))) continue;
+          // bounds may have shrunk while scanning nearer leaves
+          const float mc = c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3;
+          if (!__ballot_sync(FULL, active && mc <= list_worst(L))) continue;
+          const int64_t start = (int64_t)(lbase + c) * ix.leaf;
+          const int cnt = (int)min((int64_t)ix.leaf, ix.n - start);
+          ++leaves;
+          // one coalesced load of the leaf into shared memory, then broadcast
+          // reads (one point per iteration: the insertion is inlined at this
+          // single site, and unrolling it costs more in instruction fetch
+          // than it saves)
+          __syncwarp();
+          if (lane < cnt) ps.rec[lane] = __ldg(ix.rec + start + lane);
+          __syncwarp();
+          if (active) {
+            for (int k = 0; k < cnt; ++k) {
+              const float4 cr = ps.rec[k];
+              const float d = d2_point(cr, qx, qy, qz);
+              if (d <= list_worst(L)) list_consider_unique(L, d, (int32_t)(start + k), cr.w, ix.perm);
+            }
           }
         }
-      }
-    } else {
-      // push the needed children farthest-first, descend into the nearest
-      int first = -1;
+      } else {
+        // descend into the nearest needed child; lanes 0-3 push the others
+        // (order position t by lane t), farthest deepest so the nearest pops first
+        unsigned om = 0;  // bit t: the child at order position t is needed
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int c = (int)((order >> (2 * t)) & 3u);
-        if ((needm & (1u << c)) && first < 0) first = c;
-      }
-      if (sp + 3 > PSTACK) return false;
-      const uint32_t code = (uint32_t)(lvl + 1) << 28;
-#pragma unroll
-      for (int t = 3; t >= 0; --t) {
-        const int c = (int)((order >> (2 * t)) & 3u);
-        if ((needm & (1u << c)) && c != first) {
-          if (lane == 0) ps.code[sp] = code | (base + c);
-          ++sp;
+        for (int t = 0; t < 4; ++t) om |= ((needm >> ((order >> (2 * t)) & 3u)) & 1u) << t;
+        const int tf = __ffs(om) - 1;
+        const unsigned rest = om & (om - 1u);
+        if (sp + 3 > PSTACK) return false;
+        const uint32_t child0 = 4u * G + 1u;
+        if (lane < 4 && ((rest >> lane) & 1u)) {
+          const int slot = sp + __popc(rest >> (lane + 1));
+          ps.code[slot] = ((uint32_t)(lvl + 1) << 28) | (child0 + ((order >> (2 * lane)) & 3u));
         }
-      }
-      __syncwarp();
-      if (first >= 0) {
+        sp += __popc(rest);
+        __syncwarp();
         lvl = lvl + 1;
-        j = base + first;
+        G = child0 + ((order >> (2 * tf)) & 3u);
         continue;
       }
     }
@@ -509,18 +516,17 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
       --sp;
       const uint32_t code = ps.code[sp];
       const int plvl = (int)(code >> 28);
-      const uint32_t pj = code & 0x0fffffffu;
-      // the node's box: lane (pj & 3) of its parent's group
-      const float* pg = reinterpret_cast<const float*>(
-          ix.groups + (size_t)GROUP_F4 * (size_t)(group_offset(plvl - 1) + (pj >> 2)));
-      const int c = (int)(pj & 3u);
+      const uint32_t pG = code & 0x0fffffffu;
+      // the node's box: lane (pG - 1) & 3 of its parent's group (pG - 1) >> 2
+      const float* pg = reinterpret_cast<const float*>(ix.groups + (size_t)GROUP_F4 * ((pG - 1u) >> 2));
+      const int c = (int)((pG - 1u) & 3u);
       float md = INF;
       if (active)
         md = d2_box(__ldg(pg + 0 + c), __ldg(pg + 4 + c), __ldg(pg + 8 + c), __ldg(pg + 12 + c),
                     __ldg(pg + 16 + c), __ldg(pg + 20 + c), qx, qy, qz);
       if (__ballot_sync(FULL, active && md <= list_worst(L))) {
         lvl = plvl;
-        j = pj;
+        G = pG;
         found = true;
         break;
       }
