@@ -124,8 +124,10 @@ __device__ __forceinline__ float klist_worst(const KList<K>& L) {
 //
 // Cost.  An insertion is the hot divergent path of the packet walk (about
 // 80 per ray step at 20M points), so its common case touches no memory and
-// takes no branch: one equality scan over the distances, then one
-// compare-and-select pass that slides the new entry into place.  A
+// takes no branch: one equality scan over the distances, then one select
+// pass that slides the new entry into place, with all ten comparisons
+// independent of each other (a serial compare-and-swap chain would leave
+// the warp waiting on each result).  A
 // duplicate of a present point has the same record and query, hence the
 // same d2 bits, so the equality scan catches duplicates together with exact
 // distance ties; both go to the ordered path that compares cloud indices.
@@ -152,17 +154,19 @@ struct KSet {
       consider_ordered(dd, ss, perm);
       return;
     }
-    // no entry at distance dd: order by d2 alone
+    // no entry at distance dd: order by d2 alone.  The list is sorted, so
+    // the predicates d[j] > dd are false then true; every slot takes its own
+    // entry, the new one, or its left neighbour's (no serial chain)
+    bool gt[KNN];
 #pragma unroll
-    for (int j = 0; j < KNN; ++j) {
-      const bool sw = d[j] > dd;
-      const float td = d[j];
-      const int32_t ts = s[j];
-      d[j] = sw ? dd : td;
-      s[j] = sw ? ss : ts;
-      dd = sw ? td : dd;
-      ss = sw ? ts : ss;
+    for (int j = 0; j < KNN; ++j) gt[j] = d[j] > dd;
+#pragma unroll
+    for (int j = KNN - 1; j > 0; --j) {
+      d[j] = gt[j] ? (gt[j - 1] ? d[j - 1] : dd) : d[j];
+      s[j] = gt[j] ? (gt[j - 1] ? s[j - 1] : ss) : s[j];
     }
+    d[0] = gt[0] ? dd : d[0];
+    s[0] = gt[0] ? ss : s[0];
   }
 
   // Equal distances present: skip a duplicate, else insert by (d2, cloud index).
