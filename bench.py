@@ -349,7 +349,8 @@ def main():
             e2e = total_rays / float(np.mean(e2e_t)) / 1e6
             h2d = len(views) * ctypes.sizeof(_abi.RmView)
             d2h = total_rays * 16
-            log("e2e %.1f ms" % (1e3 * float(np.mean(e2e_t))))
+            log("e2e %.1f ms (last call's batched launch %.1f ms on the device)" % (
+                1e3 * float(np.mean(e2e_t)), r.stats()["kernel_ms"]))
 
         # ---- forward / forward+backward per 1067x690 view on a 1M-point cloud
         fb = {"fwd_ms": None, "fwdbwd_ms": None, "ratio": None}

@@ -18,9 +18,11 @@
  *   - A context owns all device memory it allocates; caller pointers are
  *     borrowed for the duration of a call only.
  *   - `loc` says where caller buffers live: RM_HOST (pageable or pinned host
- *     memory; the call copies and synchronises) or RM_DEVICE (device
+ *     memory; the call synchronises before it returns) or RM_DEVICE (device
  *     pointers on the context's device; the call is asynchronous on the
- *     context's stream, use rm_synchronize).
+ *     context's stream, use rm_synchronize).  Render outputs in pinned host
+ *     memory are written by the kernel directly; pageable ones are staged on
+ *     the device and copied after the kernel.
  *   - One context per host thread.  Contexts are independent.
  *   - Images are row-major W x H with row 0 at the BOTTOM (the reference
  *     renders into an OpenGL texture whose row 0 is the bottom row); the

@@ -113,6 +113,34 @@ struct FrameStaging {
   int32_t* steps;
 };
 
+// Device-visible address of a caller's host buffer when it is pinned
+// (page-locked and mapped into the device's address space), else nullptr.
+// The marchers write such buffers directly over the CPU-GPU link while they
+// run, so a host-side frame costs no staging buffer and no copy phase after
+// the kernel; pageable buffers keep the stage-then-copy path.
+void* pinned_device_ptr(void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return at.devicePointer;
+}
+
+// Every non-NULL output of `out` pinned?  Then `f` gets their device-visible
+// addresses.
+bool frame_pinned(const rm_frame& out, FrameStaging* f) {
+  FrameStaging g{nullptr, nullptr, nullptr, nullptr};
+  if (out.rgbd && !(g.rgbd = (float4*)pinned_device_ptr(out.rgbd))) return false;
+  if (out.hit && !(g.hit = (int32_t*)pinned_device_ptr(out.hit))) return false;
+  if (out.depth && !(g.depth = (float*)pinned_device_ptr(out.depth))) return false;
+  if (out.steps && !(g.steps = (int32_t*)pinned_device_ptr(out.steps))) return false;
+  *f = g;
+  return true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -367,7 +395,8 @@ rm_status rm_render(rm_ctx* ctx, const rm_view* view, const rm_frame* out, int32
     if (!view_ok(*view, &why)) return fail(c, RM_ERR_INVALID, "rm_render: " + why);
     size_t npix = (size_t)view->width * view->height;
     FrameStaging f{(float4*)out->rgbd, out->hit, out->depth, out->steps};
-    if (loc == RM_HOST) {
+    const bool direct = loc == RM_HOST && c.n > 0 && frame_pinned(*out, &f);
+    if (loc == RM_HOST && !direct) {
       c.frame_bufs.reserve(npix * 28);
       char* b = c.frame_bufs.ptr<char>();
       f.rgbd = out->rgbd ? (float4*)b : nullptr;
@@ -390,10 +419,12 @@ rm_status rm_render(rm_ctx* ctx, const rm_view* view, const rm_frame* out, int32
       CK(cudaEventRecord(c.ev1, c.stream));
     }
     if (loc == RM_HOST) {
-      if (out->rgbd) CK(cudaMemcpyAsync(out->rgbd, f.rgbd, npix * 16, cudaMemcpyDeviceToHost, c.stream));
-      if (out->hit) CK(cudaMemcpyAsync(out->hit, f.hit, npix * 4, cudaMemcpyDeviceToHost, c.stream));
-      if (out->depth) CK(cudaMemcpyAsync(out->depth, f.depth, npix * 4, cudaMemcpyDeviceToHost, c.stream));
-      if (out->steps) CK(cudaMemcpyAsync(out->steps, f.steps, npix * 4, cudaMemcpyDeviceToHost, c.stream));
+      if (!direct) {
+        if (out->rgbd) CK(cudaMemcpyAsync(out->rgbd, f.rgbd, npix * 16, cudaMemcpyDeviceToHost, c.stream));
+        if (out->hit) CK(cudaMemcpyAsync(out->hit, f.hit, npix * 4, cudaMemcpyDeviceToHost, c.stream));
+        if (out->depth) CK(cudaMemcpyAsync(out->depth, f.depth, npix * 4, cudaMemcpyDeviceToHost, c.stream));
+        if (out->steps) CK(cudaMemcpyAsync(out->steps, f.steps, npix * 4, cudaMemcpyDeviceToHost, c.stream));
+      }
       check_kernel_errors(c);
     }
     c.stats.kernel_ms = -1.0f;
@@ -514,7 +545,19 @@ rm_status rm_render_batch(rm_ctx* ctx, const rm_view* views, int32_t n, const rm
     std::vector<int64_t> base(n + 1);
     int64_t items = fill_views(c, views, n, c.launch, hv, base.data());
     int64_t total = base[n];
-    if (loc == RM_HOST) {
+    bool direct = loc == RM_HOST;
+    for (int v = 0; direct && v < n; ++v) {
+      FrameStaging f;
+      if (!frame_pinned(out[v], &f)) {
+        direct = false;
+        break;
+      }
+      hv[v].rgbd = f.rgbd;
+      hv[v].hit = f.hit;
+      hv[v].depth = f.depth;
+      hv[v].steps = f.steps;
+    }
+    if (loc == RM_HOST && !direct) {
       c.frame_bufs.reserve((size_t)total * 28);
       char* b = c.frame_bufs.ptr<char>();
       for (int v = 0; v < n; ++v) {
@@ -524,7 +567,7 @@ rm_status rm_render_batch(rm_ctx* ctx, const rm_view* views, int32_t n, const rm
         hv[v].depth = out[v].depth ? (float*)(b + (size_t)total * 20 + o * 4) : nullptr;
         hv[v].steps = out[v].steps ? (int32_t*)(b + (size_t)total * 24 + o * 4) : nullptr;
       }
-    } else {
+    } else if (loc != RM_HOST) {
       for (int v = 0; v < n; ++v) {
         hv[v].rgbd = (float4*)out[v].rgbd;
         hv[v].hit = out[v].hit;
@@ -535,7 +578,7 @@ rm_status rm_render_batch(rm_ctx* ctx, const rm_view* views, int32_t n, const rm
     c.views.reserve((size_t)n * sizeof(ViewDev));
     enqueue_batch(c, n, items, c.launch);
     if (loc == RM_HOST) {
-      for (int v = 0; v < n; ++v) {
+      for (int v = 0; !direct && v < n; ++v) {
         size_t np = (size_t)views[v].width * views[v].height;
         if (out[v].rgbd) CK(cudaMemcpyAsync(out[v].rgbd, hv[v].rgbd, np * 16, cudaMemcpyDeviceToHost, c.stream));
         if (out[v].hit) CK(cudaMemcpyAsync(out[v].hit, hv[v].hit, np * 4, cudaMemcpyDeviceToHost, c.stream));

@@ -202,3 +202,59 @@ def test_errors_are_status_codes_not_exits():
         r.set_cloud(np.array([[0, np.nan, 0]], np.float32)) or r.build_index()
     with pytest.raises(RmError, match="RM_ERR_INVALID"):
         r.set_launch(8, 8, 1, 4)
+
+
+def test_pinned_host_frames_equal_device_frames(scene100k):
+    """Host frames in pinned memory are written by the kernel directly; the
+    result must equal device frames (and pageable host frames) bit for bit."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from renderer_ray_marching_gb300 import _abi
+    sc, _ = scene100k
+    r, _, _ = make_renderer(sc.xyz, sc.rgb)
+    views = views_from_specs(syn.make_views(3, seed=17, boxes=sc.boxes, resolutions=[(160, 120), (97, 61)]))
+    cviews = (_abi.RmView * len(views))(*[v.to_c() for v in views])
+    fields = (("rgbd", 4, torch.float32), ("hit", 1, torch.int32), ("depth", 1, torch.float32),
+              ("steps", 1, torch.int32))
+
+    def frames(kind):
+        arr = (_abi.RmFrame * len(views))()
+        keep = []
+        for i, v in enumerate(views):
+            b = {}
+            for name, ch, dt in fields:
+                shape = (v.height, v.width, ch) if ch > 1 else (v.height, v.width)
+                if kind == "device":
+                    t = torch.full(shape, -3, dtype=dt, device="cuda:0")
+                else:
+                    t = torch.full(shape, -3, dtype=dt)
+                    if kind == "pinned":
+                        t = t.pin_memory()
+                setattr(arr[i], name, t.data_ptr())
+                b[name] = t
+            keep.append(b)
+        return arr, keep
+
+    def host(keep):
+        return [{k: t.cpu().numpy().copy() for k, t in b.items()} for b in keep]
+
+    out = {}
+    for kind in ("device", "pinned", "pageable"):
+        arr, keep = frames(kind)
+        loc = _abi.RM_DEVICE if kind == "device" else _abi.RM_HOST
+        _abi.check(r._lib, r._h, r._lib.rm_render_batch(r._h, cviews, len(views), arr, loc))
+        r.synchronize()
+        out["batch_" + kind] = host(keep)
+        arr, keep = frames(kind)
+        for i in range(len(views)):
+            _abi.check(r._lib, r._h, r._lib.rm_render(r._h, ctypes.byref(cviews[i]), ctypes.byref(arr[i]), loc))
+        r.synchronize()
+        out["plain_" + kind] = host(keep)
+    ref = out["batch_device"]
+    for key, frames_ in out.items():
+        for a, b in zip(ref, frames_):
+            for name in ("hit", "steps"):
+                assert np.array_equal(a[name], b[name]), (key, name)
+            for name in ("rgbd", "depth"):
+                assert np.array_equal(a[name].view(np.int32), b[name].view(np.int32)), (key, name)
+    r.close()
