@@ -49,8 +49,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--points", type=int, default=20_000_000)
-    ap.add_argument("--views", type=int, default=256)
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
+                    help="c2: 20M points, 40 boxes, 256 mixed-resolution views (the headline); "
+                         "c4: 100M points, per-surface density log-uniform over 100x, 1024 views at 1067x690, "
+                         "fwd+bwd on 64 of them")
+    ap.add_argument("--points", type=int, default=None)
+    ap.add_argument("--views", type=int, default=None)
     ap.add_argument("--cpu-rays", type=int, default=2_000_000,
                     help="rays per CPU-baseline sample (about 12 s of 16-core CPU work at 20M points)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -77,15 +81,42 @@ def dist_info():
     return ws, rank, local
 
 
+WORKLOADS = {
+    # points, boxes, per-surface density range, views, resolutions (None: the
+    # reference's README intrinsics, 1067x690)
+    "c2": dict(points=20_000_000, boxes=40, density=1.0, views=256, res=RES),
+    "c4": dict(points=100_000_000, boxes=12, density=100.0, views=1024, res=None),
+}
+
+
+def workload_spec(args):
+    w = dict(WORKLOADS[getattr(args, "workload", "c2")])
+    if getattr(args, "points", None):
+        w["points"] = args.points
+    if getattr(args, "views", None):
+        w["views"] = args.views
+    if getattr(args, "resolution", None):
+        ww, hh = (int(x) for x in args.resolution.lower().split("x"))
+        w["res"] = [(ww, hh)]
+    return w
+
+
 def workload(args, rank):
     from renderer_ray_marching_gb300 import synthetic as syn, views_from_specs
-    sc = syn.make_scene(args.points, n_boxes=40, seed=2000 + rank)
-    res = RES
-    if getattr(args, "resolution", None):
-        w, h = (int(x) for x in args.resolution.lower().split("x"))
-        res = [(w, h)]
-    specs = syn.make_views(args.views, seed=3000 + rank, boxes=sc.boxes, resolutions=res)
+    w = workload_spec(args)
+    sc = syn.make_scene(w["points"], n_boxes=w["boxes"], seed=2000 + rank, density_range=w["density"])
+    specs = syn.make_views(w["views"], seed=3000 + rank, boxes=sc.boxes, resolutions=w["res"])
     return sc, views_from_specs(specs)
+
+
+def workload_name(args, n_points, n_views):
+    w = workload_spec(args)
+    if w["res"] is None:
+        shape = "%d views at 1067x690 (fx=803.8)" % n_views
+    else:
+        shape = "%d views (%s, fx=0.75W)" % (n_views, "/".join("%dx%d" % r for r in w["res"]))
+    dens = "" if w["density"] <= 1.0 else ", per-surface density log-uniform over %gx" % w["density"]
+    return "batched render of %s over a %d-point synthetic room, %d boxes%s" % (shape, n_points, w["boxes"], dens)
 
 
 class Clocks:
@@ -215,8 +246,8 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * float(np.mean(times)), 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched render, %d points, %d views from {640x480, 1068x690, 1920x1080}" % (
-                sc.xyz.shape[0], len(vp)), "points": int(sc.xyz.shape[0]), "views": len(vp)},
+            "config": {"workload": workload_name(args, sc.xyz.shape[0], len(vp)), "points": int(sc.xyz.shape[0]),
+                       "views": len(vp)},
             "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
@@ -355,7 +386,10 @@ def main():
         # ---- forward / forward+backward per 1067x690 view on a 1M-point cloud
         fb = {"fwd_ms": None, "fwdbwd_ms": None, "ratio": None}
         if not args.skip_fwdbwd:
-            fb = fwd_bwd(args, dev, stream, rank)
+            if args.workload == "c4":
+                fb = fwd_bwd(args, dev, stream, rank, scene=sc, views=views[:64])
+            else:
+                fb = fwd_bwd(args, dev, stream, rank)
             log("fwd/bwd %s" % fb)
         r.close()
 
@@ -368,8 +402,7 @@ def main():
     out = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(t_step, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": "batched render of %d views (640x480/1068x690/1920x1080, fx=0.75W) over a %d-point "
-                                  "synthetic room, 40 boxes" % (len(views), sc.xyz.shape[0]),
+           "config": {"workload": workload_name(args, sc.xyz.shape[0], len(views)),
                       "points": int(sc.xyz.shape[0]), "views": len(views), "rays_per_step": int(total_rays),
                       "l2": "inputs larger than L2 (cloud + index >= 0.8 GB), no flush",
                       "launch": tune, "parallelism": "replicas" if ws > 1 else "single"},
@@ -409,13 +442,15 @@ def main():
         tdist.destroy_process_group()
 
 
-def fwd_bwd(args, dev, stream, rank):
-    """Forward (plain render) and forward + loss gradient + backward per
-    1067x690 view over 16 views of a 1M-point cloud."""
+def fwd_bwd(args, dev, stream, rank, scene=None, views=None):
+    """Forward (plain render) and forward + loss gradient + backward per view:
+    by default 16 1067x690 views of a 1M-point cloud; or the given scene and
+    views.  Targets come from a copy with xyz + N(0, 5 mm) and colour +-30."""
     import torch
     from renderer_ray_marching_gb300 import Renderer, _abi, synthetic as syn, views_from_specs
-    sc = syn.make_scene(1_000_000, n_boxes=12, seed=4000 + rank)
-    views = views_from_specs(syn.make_views(16, seed=4100 + rank, boxes=sc.boxes))
+    sc = scene if scene is not None else syn.make_scene(1_000_000, n_boxes=12, seed=4000 + rank)
+    if views is None:
+        views = views_from_specs(syn.make_views(16, seed=4100 + rank, boxes=sc.boxes))
     rng = np.random.default_rng(5)
     xt = (sc.xyz + rng.normal(0, 0.005, sc.xyz.shape)).astype(np.float32)
     ct = np.clip(sc.rgb.astype(np.int32) + rng.integers(-30, 31, sc.rgb.shape), 0, 255).astype(np.uint8)
