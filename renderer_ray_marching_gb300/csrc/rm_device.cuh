@@ -65,6 +65,56 @@ __device__ __forceinline__ float d2_box(float lx, float ly, float lz, float hx, 
   return __fmaf_rn(gz, gz, __fmaf_rn(gx, gx, __fmul_rn(gy, gy)));
 }
 
+// Paired FP32 arithmetic (sm_100 and later): two IEEE round-to-nearest
+// operations per instruction, so a paired expression gives the same bits as
+// the scalar one.
+__device__ __forceinline__ unsigned long long f2_pack(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+// d2_box of the four children of a group (same operations, same bits): the
+// group's structure-of-arrays lanes pair up as (0, 1) and (2, 3); only the
+// max has no paired form
+__device__ __forceinline__ void d2_box4(float4 lx, float4 ly, float4 lz, float4 hx, float4 hy, float4 hz,
+                                        unsigned long long qx2, unsigned long long qy2, unsigned long long qz2,
+                                        float& m0, float& m1, float& m2, float& m3) {
+  float a0, a1, a2, a3, b0, b1, b2, b3;
+  unsigned long long g01[3], g23[3];
+  const float4* lo[3] = {&lx, &ly, &lz};
+  const float4* hi[3] = {&hx, &hy, &hz};
+  const unsigned long long q2[3] = {qx2, qy2, qz2};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    f2_unpack(f2_sub(f2_pack(lo[a]->x, lo[a]->y), q2[a]), a0, a1);
+    f2_unpack(f2_sub(f2_pack(lo[a]->z, lo[a]->w), q2[a]), a2, a3);
+    f2_unpack(f2_sub(q2[a], f2_pack(hi[a]->x, hi[a]->y)), b0, b1);
+    f2_unpack(f2_sub(q2[a], f2_pack(hi[a]->z, hi[a]->w)), b2, b3);
+    g01[a] = f2_pack(fmaxf(fmaxf(a0, b0), 0.0f), fmaxf(fmaxf(a1, b1), 0.0f));
+    g23[a] = f2_pack(fmaxf(fmaxf(a2, b2), 0.0f), fmaxf(fmaxf(a3, b3), 0.0f));
+  }
+  f2_unpack(f2_fma(g01[2], g01[2], f2_fma(g01[0], g01[0], f2_mul(g01[1], g01[1]))), m0, m1);
+  f2_unpack(f2_fma(g23[2], g23[2], f2_fma(g23[0], g23[0], f2_mul(g23[1], g23[1]))), m2, m3);
+}
+
 // k nearest candidates kept sorted by (d2, cloud index) ascending.
 template <int K>
 struct KList {
@@ -156,17 +206,19 @@ struct KSet {
     }
     // no entry at distance dd: order by d2 alone.  The list is sorted, so
     // the predicates d[j] > dd are false then true; every slot takes its own
-    // entry, the new one, or its left neighbour's (no serial chain)
-    bool gt[KNN];
-#pragma unroll
-    for (int j = 0; j < KNN; ++j) gt[j] = d[j] > dd;
+    // entry, the new one, or its left neighbour's (no serial chain).  Each
+    // comparison is written where it is used: a form that first stored the
+    // ten predicates in a bool array gave wrong results on the GPU in one
+    // kernel although the same C++ is correct on the CPU.
 #pragma unroll
     for (int j = KNN - 1; j > 0; --j) {
-      d[j] = gt[j] ? (gt[j - 1] ? d[j - 1] : dd) : d[j];
-      s[j] = gt[j] ? (gt[j - 1] ? s[j - 1] : ss) : s[j];
+      const bool g = d[j] > dd, gp = d[j - 1] > dd;
+      d[j] = g ? (gp ? d[j - 1] : dd) : d[j];
+      s[j] = g ? (gp ? s[j - 1] : ss) : s[j];
     }
-    d[0] = gt[0] ? dd : d[0];
-    s[0] = gt[0] ? ss : s[0];
+    const bool g0 = d[0] > dd;
+    d[0] = g0 ? dd : d[0];
+    s[0] = g0 ? ss : s[0];
   }
 
   // Equal distances present: skip a duplicate, else insert by (d2, cloud index).
@@ -429,6 +481,7 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
   const unsigned central = act & 0x00181800u;
   const int leader = __ffs(central ? central : act) - 1;
   const uint32_t last_first = (uint32_t)group_offset(ix.depth - 1);  // first group of level depth-1
+  const unsigned long long qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
   int sp = 0;
   int lvl = 0;
   uint32_t G = 0;
@@ -441,10 +494,7 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
     {
       float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
       float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
-      m0 = d2_box(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, qx, qy, qz);
-      m1 = d2_box(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, qx, qy, qz);
-      m2 = d2_box(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, qx, qy, qz);
-      m3 = d2_box(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, qx, qy, qz);
+      d2_box4(lx, ly, lz, hx, hy, hz, qx2, qy2, qz2, m0, m1, m2, m3);
     }
     // needed children: one OR-reduction of every active lane's 4-bit vote
     // (idle lanes do not vote: their bound may be +inf, and inf <= inf)
