@@ -71,16 +71,15 @@ __device__ __forceinline__ float clip_exit(const Ray& r, const ClipBox& e) {
 }
 
 constexpr int WARPS_PER_CTA = 4;
-using WarpSmem = PacketStack;
 
 struct MarchParams {
   ClipBox clip;
   int search;  // 1: warp packet traversal, 0: one walk per lane
 };
 
-// View as seen by the marcher.
+// View as seen by the marcher (kept per warp in shared memory).
 struct ViewArgs {
-  const float* m;
+  float m[16];
   int32_t width, height;
   float pane;
   float4* rgbd;
@@ -92,9 +91,17 @@ struct ViewArgs {
 // counters: [0] steps, [1] rays, [2] hits, [3] search errors,
 //           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets,
 //           [7] nodes expanded by packets, [8] warp steps, [9] warp steps split in two packets
-struct LaneCounters {
-  unsigned steps = 0, rays = 0, hits = 0, bad = 0, coop = 0, solo = 0, leaves = 0, nodes = 0,
-           wsteps = 0, split = 0;
+enum { C_STEPS, C_RAYS, C_HITS, C_BAD, C_COOP, C_SOLO, C_LEAVES, C_NODES, C_WSTEPS, C_SPLIT, C_N };
+
+// Per-warp shared state.  The view of the current item and the statistics
+// live here rather than in registers: they are read or bumped at a ray's
+// start and end (or once per warp step by one lane), and every register the
+// stepping loop does not hold lets more warps stay resident (the marcher is
+// bound by instruction latency, so resident warps are what hides it).
+struct WarpSmem {
+  PacketStack ps;
+  ViewArgs v;                   // warp-uniform; written by lane 0 per item
+  unsigned long long cnt[C_N];  // this warp's statistics
 };
 
 __device__ __forceinline__ float warp_min(float v) {
@@ -104,7 +111,10 @@ __device__ __forceinline__ float warp_min(float v) {
 }
 
 __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs& v, int64_t pix, int32_t s,
-                                             float depth, int32_t steps) {
+                                             float depth, int32_t steps, unsigned long long* cnt) {
+  atomicAdd(cnt + C_STEPS, (unsigned long long)steps);
+  atomicAdd(cnt + C_RAYS, 1ull);
+  if (s >= 0) atomicAdd(cnt + C_HITS, 1ull);
   if (s >= 0) {
     float4 c = __ldg(ix.col + s);
     c.w = depth;  // colour with the depth in .w (src/ray_marching.cu:85-89)
@@ -122,8 +132,9 @@ __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs&
 // Marches every ray of one item (origin x0, y0; tile_w x tile_h*rpl pixels)
 // of view v.  All 32 lanes call it.  SEARCH: 1 packet traversal, 0 per lane.
 template <int SEARCH>
-__device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0, int tile_w,
-                           int tile_h, int rpl, const MarchParams& mp, WarpSmem& sm, LaneCounters& cnt) {
+__device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int tile_h, int rpl,
+                           const MarchParams& mp, WarpSmem& sm) {
+  const ViewArgs& v = sm.v;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -161,9 +172,7 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
 
     bool stepping = has && !(t > t_stop);  // past the exit bound: a miss (culled)
     if (has && !stepping) {
-      write_result(ix, v, pix, -1, 0.0f, nsteps);
-      cnt.steps += nsteps;
-      cnt.rays += 1;
+      write_result(ix, v, pix, -1, 0.0f, nsteps, sm.cnt);
       has = false;
     }
     float px = __fmaf_rn(r.dx, t, r.ox);
@@ -178,22 +187,22 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
       float bmin = warp_min(stepping ? L.worst() : INFINITY);
       bool tight = stepping && L.worst() <= 64.0f * bmin;
       unsigned lv = 0, nd = 0;
-      if (!packet_knn(ix, tight, px, py, pz, L, sm, lv, nd)) cnt.bad += tight ? 1 : 0;
+      if (!packet_knn(ix, tight, px, py, pz, L, sm.ps, lv, nd) && tight) atomicAdd(sm.cnt + C_BAD, 1ull);
       bool rest = stepping && !tight;
       if (__ballot_sync(FULL, rest)) {
-        if (!packet_knn(ix, rest, px, py, pz, L, sm, lv, nd)) cnt.bad += rest ? 1 : 0;
-        cnt.split += lane == 0 ? 1 : 0;
+        if (!packet_knn(ix, rest, px, py, pz, L, sm.ps, lv, nd) && rest) atomicAdd(sm.cnt + C_BAD, 1ull);
+        if (lane == 0) sm.cnt[C_SPLIT] += 1;
       }
-      cnt.leaves += lane == 0 ? lv : 0;
-      cnt.nodes += lane == 0 ? nd : 0;
       const unsigned any_step = __ballot_sync(FULL, stepping);  // every lane votes
-      cnt.wsteps += (lane == 0 && any_step) ? 1 : 0;
+      if (lane == 0) {
+        sm.cnt[C_LEAVES] += lv;
+        sm.cnt[C_NODES] += nd;
+        sm.cnt[C_WSTEPS] += any_step ? 1 : 0;
+      }
     } else if (stepping) {
-      if (!knn_search(ix, px, py, pz, L)) cnt.bad += 1;
+      if (!knn_search(ix, px, py, pz, L)) atomicAdd(sm.cnt + C_BAD, 1ull);
     }
     if (stepping) {
-      if (SEARCH == 1) cnt.coop += 1;
-      else cnt.solo += 1;
       int32_t s;
       float step = L.step_value(ix, &s);
       ++nsteps;
@@ -209,29 +218,34 @@ __device__ void march_item(const IndexDev& ix, const ViewArgs& v, int x0, int y0
         fin = true;
       }
       if (fin) {
-        write_result(ix, v, pix, hs, hd, nsteps);
-        cnt.steps += nsteps;
-        cnt.rays += 1;
-        cnt.hits += hs >= 0 ? 1 : 0;
+        write_result(ix, v, pix, hs, hd, nsteps, sm.cnt);
         has = false;
       }
     }
   }
 }
 
-__device__ __forceinline__ void flush_counters(LaneCounters& c, unsigned long long* counters) {
-  unsigned long long v[10] = {c.steps, c.rays, c.hits, c.bad, c.coop, c.solo, c.leaves, c.nodes, c.wsteps, c.split};
-#pragma unroll
-  for (int k = 0; k < 10; ++k) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], off);
-  }
-  if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-    for (int k = 0; k < 10; ++k)
-      if (v[k]) atomicAdd(counters + k, v[k]);
+__device__ __forceinline__ void clear_counters(WarpSmem& sm) {
+  const int lane = threadIdx.x & 31;
+  if (lane < C_N) sm.cnt[lane] = 0ull;
+  __syncwarp();
+}
+
+// Adds the warp's statistics to the launch's counters.  Lane-steps are the
+// rays' step counts; they are reported as packet or per-lane lane-steps by
+// search mode.
+template <int SEARCH>
+__device__ __forceinline__ void flush_counters(WarpSmem& sm, unsigned long long* counters) {
+  __syncwarp();
+  const int lane = threadIdx.x & 31;
+  if (lane < C_N) {
+    unsigned long long v = lane == C_COOP ? (SEARCH == 1 ? sm.cnt[C_STEPS] : 0ull)
+                         : lane == C_SOLO ? (SEARCH == 0 ? sm.cnt[C_STEPS] : 0ull)
+                         : sm.cnt[lane];
+    if (v) atomicAdd(counters + lane, v);
   }
 }
+
 
 struct PlainArgs {
   float m[16];
@@ -253,20 +267,24 @@ k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __re
   int tiles_x = (a.width + 7) / 8;
   int tile = blockIdx.x * WARPS_PER_CTA + warp;
   int tiles = tiles_x * ((a.height + 3) / 4);
-  LaneCounters cnt;
+  WarpSmem& sm = smem[warp];
+  clear_counters(sm);
   if (tile < tiles) {
-    ViewArgs v;
-    v.m = a.m;
-    v.width = a.width;
-    v.height = a.height;
-    v.pane = view_pane(a.width, a.fov);
-    v.rgbd = a.rgbd;
-    v.hit = a.hit;
-    v.depth = a.depth;
-    v.steps = a.steps;
-    march_item<SEARCH>(ix, v, (tile % tiles_x) * 8, (tile / tiles_x) * 4, 8, 4, 1, mp, smem[warp], cnt);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) sm.v.m[k] = a.m[k];
+      sm.v.width = a.width;
+      sm.v.height = a.height;
+      sm.v.pane = view_pane(a.width, a.fov);
+      sm.v.rgbd = a.rgbd;
+      sm.v.hit = a.hit;
+      sm.v.depth = a.depth;
+      sm.v.steps = a.steps;
+    }
+    __syncwarp();
+    march_item<SEARCH>(ix, (tile % tiles_x) * 8, (tile / tiles_x) * 4, 8, 4, 1, mp, sm);
   }
-  flush_counters(cnt, counters);
+  flush_counters<SEARCH>(sm, counters);
 }
 
 // ---------------------------------------------------------------- batched
@@ -303,7 +321,8 @@ k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __re
               unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  LaneCounters cnt;
+  WarpSmem& sm = smem[warp];
+  clear_counters(sm);
   while (true) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(queue, 1ull);
@@ -312,20 +331,23 @@ k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __re
     int iv = find_view(a.views, a.nviews, (int64_t)it);
     const ViewDev& V = a.views[iv];
     int64_t local = (int64_t)it - V.tile_base;
-    ViewArgs v;
-    v.m = V.m;
-    v.width = V.width;
-    v.height = V.height;
-    v.pane = V.pane;
-    v.rgbd = V.rgbd;
-    v.hit = V.hit;
-    v.depth = V.depth;
-    v.steps = V.steps;
+    __syncwarp();  // the previous item's readers of sm.v are done
+    if (lane < 16) sm.v.m[lane] = V.m[lane];
+    if (lane == 0) {
+      sm.v.width = V.width;
+      sm.v.height = V.height;
+      sm.v.pane = V.pane;
+      sm.v.rgbd = V.rgbd;
+      sm.v.hit = V.hit;
+      sm.v.depth = V.depth;
+      sm.v.steps = V.steps;
+    }
+    __syncwarp();
     int x0 = (int)(local % V.tiles_x) * a.tile_w;
     int y0 = (int)(local / V.tiles_x) * (a.tile_h * a.rpl);
-    march_item<SEARCH>(ix, v, x0, y0, a.tile_w, a.tile_h, a.rpl, mp, smem[warp], cnt);
+    march_item<SEARCH>(ix, x0, y0, a.tile_w, a.tile_h, a.rpl, mp, sm);
   }
-  flush_counters(cnt, counters);
+  flush_counters<SEARCH>(sm, counters);
 }
 
 // ---------------------------------------------------------------- host side
@@ -379,6 +401,7 @@ void launch_render_plain(Ctx& c, const rm_view& v, float4* rgbd, int32_t* hit, f
   if (mp.search == 1) {
     if (cps >= 8) go(k_march_plain<1, 8>);
     else if (cps >= 6) go(k_march_plain<1, 6>);
+    else if (cps >= 5) go(k_march_plain<1, 5>);
     else go(k_march_plain<1, 4>);
   } else {
     go(k_march_plain<0, 4>);
@@ -409,6 +432,7 @@ void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
   if (mp.search == 1) {
     if (cps >= 8) go(k_march_batch<1, 8>);
     else if (cps >= 6) go(k_march_batch<1, 6>);
+    else if (cps >= 5) go(k_march_batch<1, 5>);
     else go(k_march_batch<1, 4>);
   } else {
     go(k_march_batch<0, 4>);
@@ -436,6 +460,7 @@ void launch_render_batch_queue(Ctx& c, ViewDev* views_dev, int n, int64_t total_
   if (mp.search == 1) {
     if (cps >= 8) go(k_march_batch<1, 8>);
     else if (cps >= 6) go(k_march_batch<1, 6>);
+    else if (cps >= 5) go(k_march_batch<1, 5>);
     else go(k_march_batch<1, 4>);
   } else {
     go(k_march_batch<0, 4>);
