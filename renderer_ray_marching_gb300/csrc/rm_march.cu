@@ -187,12 +187,16 @@ __device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int t
       float bmin = warp_min(stepping ? L.worst() : INFINITY);
       bool tight = stepping && L.worst() <= 64.0f * bmin;
       unsigned lv = 0, nd = 0;
-      if (!packet_knn(ix, tight, px, py, pz, L, sm.ps, lv, nd) && tight) atomicAdd(sm.cnt + C_BAD, 1ull);
-      bool rest = stepping && !tight;
-      if (__ballot_sync(FULL, rest)) {
-        if (!packet_knn(ix, rest, px, py, pz, L, sm.ps, lv, nd) && rest) atomicAdd(sm.cnt + C_BAD, 1ull);
-        if (lane == 0) sm.cnt[C_SPLIT] += 1;
+      const bool rest = stepping && !tight;
+      const bool two = __ballot_sync(FULL, rest) != 0;
+      // one call site for both packets: the walk is large, and a second
+      // inlined copy costs more in instruction fetch than the loop does
+#pragma unroll 1
+      for (int phase = 0; phase < (two ? 2 : 1); ++phase) {
+        const bool part = phase == 0 ? tight : rest;
+        if (!packet_knn(ix, part, px, py, pz, L, sm.ps, lv, nd) && part) atomicAdd(sm.cnt + C_BAD, 1ull);
       }
+      if (two && lane == 0) sm.cnt[C_SPLIT] += 1;
       const unsigned any_step = __ballot_sync(FULL, stepping);  // every lane votes
       if (lane == 0) {
         sm.cnt[C_LEAVES] += lv;
