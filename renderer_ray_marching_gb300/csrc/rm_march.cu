@@ -9,15 +9,17 @@
 // position, found by a warp packet traversal:
 //
 //   1. seed: every lane re-measures its previous step's 10 points at the new
-//      position (valid candidates, so its 10th distance is finite at once);
-//   2. the warp walks the tree once, as a unit: a node is expanded when its
-//      box lies within the current 10th distance of ANY active lane (one
-//      __ballot_sync per child), children are visited nearest-first for the
-//      leading lane, and a stack of pending boxes lives in shared memory so
-//      every pop is re-tested against the (shrinking) bounds of all lanes;
-//   3. a leaf's records are read once for the whole warp (broadcast loads)
-//      and every lane updates its own exact set, so all lanes' bounds tighten
-//      while the walk goes on.
+//      position (valid candidates, so its 10th distance is finite at once)
+//      and re-sorts them;
+//   2. the warp walks the tree once, as a unit (packet_knn): a node is
+//      expanded when its box lies within the current 10th distance of ANY
+//      active lane (one OR-reduction of 4-bit child votes), children are
+//      visited nearest-first for a leading lane, and pending nodes wait on a
+//      shared-memory stack so every pop is re-tested against the (shrinking)
+//      bounds of all lanes;
+//   3. a leaf's records are staged once for the whole warp (broadcast
+//      loads) and every lane updates its own sorted set, so all lanes'
+//      bounds tighten while the walk goes on.
 // Neighbouring rays need nearly the same leaves (at surfaces, and in open
 // space where the 10 nearest of every lane cluster around the same foot
 // point), so the warp pays for the union of their searches once instead of
@@ -28,6 +30,9 @@
 // Plain form (rm_render): one warp per 8x4 tile, four warps per CTA.
 // Batched form (rm_render_batch): a persistent kernel whose warps pull items
 // of any view from one global counter; the whole launch is a CUDA graph.
+// Both are templated on the CTAs per SM their register budget is sized for
+// (4, 5, 6 or 8); the kernel is latency-bound, so resident warps matter and
+// the per-item view and the statistics live in shared memory (WarpSmem).
 //
 // Culling.  The reference's view-frustum test is a no-op (is_inside,
 // src/ray_marching.cu:231-258, returns true); its effective culling is the
