@@ -428,6 +428,13 @@ struct PacketStack {
   float4 rec[32];  // one staged leaf (leaf size <= 32)
 };
 
+// Shared memory of the best-first walk: the depth-first stack and staged
+// leaf of PacketStack plus the queue's overflow stack.
+constexpr int PKT_OVERFLOW = 256;
+struct PacketQueue : PacketStack {
+  uint32_t over[PKT_OVERFLOW];
+};
+
 __device__ __forceinline__ void list_consider_unique(KSet& L, float d, int32_t s, float r,
                                                      const int32_t* perm) {
   (void)r;
@@ -569,6 +576,221 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
     while (sp > 0) {
       --sp;
       const uint32_t code = ps.code[sp];
+      const int plvl = (int)(code >> 28);
+      const uint32_t pG = code & 0x0fffffffu;
+      // the node's box: lane (pG - 1) & 3 of its parent's group (pG - 1) >> 2
+      const float* pg = reinterpret_cast<const float*>(ix.groups + (size_t)GROUP_F4 * ((pG - 1u) >> 2));
+      const int c = (int)((pG - 1u) & 3u);
+      float md = INF;
+      if (active)
+        md = d2_box(__ldg(pg + 0 + c), __ldg(pg + 4 + c), __ldg(pg + 8 + c), __ldg(pg + 12 + c),
+                    __ldg(pg + 16 + c), __ldg(pg + 20 + c), qx, qy, qz);
+      if (__ballot_sync(FULL, active && md <= list_worst(L))) {
+        lvl = plvl;
+        G = pG;
+        found = true;
+        break;
+      }
+    }
+    __syncwarp();
+    if (!found) break;
+  }
+  return true;
+}
+
+// Best-first form of packet_knn for the marcher.  The depth-first walk
+// finishes the leading lane's subtree before anything else, so lanes whose
+// nearest points lie in another subtree keep loose bounds (and so want
+// most leaves) for much of the walk.  Here pending nodes wait in a priority
+// queue keyed by the leading lane's box distance, and the walk always
+// continues with the nearest one; the leaves of a node at level depth-1
+// are scanned when it is expanded.  A CPU simulation of both walks on
+// recorded warp steps gave about 20% fewer leaves and 12% fewer nodes.
+// The queue is 32 entries in registers (lane i holds the i-th nearest);
+// the farthest entry of a full queue moves to an overflow stack in shared
+// memory, and if that fills as well the walk continues depth-first on the
+// bounded stack from then on.  Every pending node is still re-tested when
+// taken, so the result is exact whatever the order.
+template <class List>
+__device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float qy, float qz, List& L,
+                              PacketQueue& ps, unsigned& leaves, unsigned& nodes) {
+  const unsigned FULL = 0xffffffffu;
+  const float INF = __int_as_float(0x7f800000);
+  const int lane = threadIdx.x & 31;
+  unsigned act = __ballot_sync(FULL, active);
+  if (act == 0 || ix.n <= 0) return true;
+  // the visiting order follows one lane: a central pixel of an 8x4 tile
+  // (lanes 11, 12, 19, 20) when one is active, whose nearest-first order
+  // suits its neighbours better than a corner's
+  const unsigned central = act & 0x00181800u;
+  const int leader = __ffs(central ? central : act) - 1;
+  const uint32_t last_first = (uint32_t)group_offset(ix.depth - 1);  // first group of level depth-1
+  const unsigned long long qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
+  int sp = 0;     // depth-first stack (ps.code), used once `dfs` is set
+  int osp = 0;    // overflow stack (ps.over)
+  int qn = 0;     // register queue: lane i holds the i-th nearest pending node
+  float qkey = INF;
+  uint32_t qcode = 0;
+  bool dfs = false;
+  // queue insert (warp-uniform key and code); the farthest entry of a full
+  // queue moves to the overflow stack, and a full overflow stack switches
+  // the walk to depth-first mode on the bounded stack
+  auto spill = [&](uint32_t code) {
+    if (!dfs && osp < PKT_OVERFLOW) {
+      if (lane == 0) ps.over[osp] = code;
+      ++osp;
+    } else {
+      dfs = true;
+      if (sp < PSTACK && lane == 0) ps.code[sp] = code;
+      ++sp;
+    }
+  };
+  auto qpush = [&](float key, uint32_t code) {
+    const int pos = __popc(__ballot_sync(FULL, lane < qn && qkey <= key));
+    if (qn == 32) {
+      if (pos == 32) {
+        spill(code);
+        return;
+      }
+      spill(__shfl_sync(FULL, qcode, 31));
+    } else {
+      ++qn;
+    }
+    const float ku = __shfl_up_sync(FULL, qkey, 1);
+    const uint32_t cu = __shfl_up_sync(FULL, qcode, 1);
+    if (lane > pos) {
+      qkey = ku;
+      qcode = cu;
+    }
+    if (lane == pos) {
+      qkey = key;
+      qcode = code;
+    }
+  };
+  int lvl = 0;
+  uint32_t G = 0;
+  unsigned budget = PACKET_NODE_BUDGET;
+  while (true) {
+    ++nodes;
+    if (--budget == 0) return false;  // self-check: a walk this long means a broken bound
+    const float4* g = ix.groups + (size_t)GROUP_F4 * G;
+    float m0, m1, m2, m3;
+    {
+      float4 lx = __ldg(g + 0), ly = __ldg(g + 1), lz = __ldg(g + 2);
+      float4 hx = __ldg(g + 3), hy = __ldg(g + 4), hz = __ldg(g + 5);
+      d2_box4(lx, ly, lz, hx, hy, hz, qx2, qy2, qz2, m0, m1, m2, m3);
+    }
+    // needed children: one OR-reduction of every active lane's 4-bit vote
+    // (idle lanes do not vote: their bound may be +inf, and inf <= inf)
+    const float w = list_worst(L);
+    unsigned mine = 0;
+    if (active) mine = (m0 <= w ? 1u : 0u) | (m1 <= w ? 2u : 0u) | (m2 <= w ? 4u : 0u) | (m3 <= w ? 8u : 0u);
+    const unsigned needm = __reduce_or_sync(FULL, mine);
+    if (needm != 0) {
+      // visiting order (2 bits per position, nearest first for the leading
+      // lane); with one needed child any order will do
+      unsigned order = 0xE4u;  // 0, 1, 2, 3
+      if (needm & (needm - 1u)) {
+        float k0 = m0, k1 = m1, k2 = m2, k3 = m3;
+        int o0 = 0, o1 = 1, o2 = 2, o3 = 3;
+        RM_CSWAP_U(k0, o0, k1, o1);
+        RM_CSWAP_U(k2, o2, k3, o3);
+        RM_CSWAP_U(k0, o0, k2, o2);
+        RM_CSWAP_U(k1, o1, k3, o3);
+        RM_CSWAP_U(k1, o1, k2, o2);
+        order = __shfl_sync(FULL, (unsigned)o0 | ((unsigned)o1 << 2) | ((unsigned)o2 << 4) | ((unsigned)o3 << 6),
+                            leader);
+      }
+      if (lvl + 1 == ix.depth) {
+        const uint32_t lbase = (G - last_first) * 4u;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int c = (int)((order >> (2 * t)) & 3u);
+          if (!(needm & (1u << c))) continue;
+          // bounds may have shrunk while scanning nearer leaves
+          const float mc = c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3;
+          if (!__ballot_sync(FULL, active && mc <= list_worst(L))) continue;
+          const int64_t start = (int64_t)(lbase + c) * ix.leaf;
+          const int cnt = (int)min((int64_t)ix.leaf, ix.n - start);
+          ++leaves;
+          // one coalesced load of the leaf into shared memory, then broadcast
+          // reads (one point per iteration: the insertion is inlined at this
+          // single site, and unrolling it costs more in instruction fetch
+          // than it saves)
+          __syncwarp();
+          if (lane < cnt) ps.rec[lane] = __ldg(ix.rec + start + lane);
+          __syncwarp();
+          if (active) {
+            for (int k = 0; k < cnt; ++k) {
+              const float4 cr = ps.rec[k];
+              const float d = d2_point(cr, qx, qy, qz);
+              if (d <= list_worst(L)) list_consider_unique(L, d, (int32_t)(start + k), cr.w, ix.perm);
+            }
+          }
+        }
+      } else {
+        unsigned om = 0;  // bit t: the child at order position t is needed
+#pragma unroll
+        for (int t = 0; t < 4; ++t) om |= ((needm >> ((order >> (2 * t)) & 3u)) & 1u) << t;
+        const int tf = __ffs(om) - 1;
+        const unsigned rest = om & (om - 1u);
+        const uint32_t child0 = 4u * G + 1u;
+        const uint32_t lcode = (uint32_t)(lvl + 1) << 28;
+        if (dfs) {
+          // depth-first: descend into the nearest needed child; lanes 0-3
+          // push the others, farthest deepest so the nearest pops first
+          if (sp + 3 > PSTACK) return false;
+          if (lane < 4 && ((rest >> lane) & 1u)) {
+            const int slot = sp + __popc(rest >> (lane + 1));
+            ps.code[slot] = lcode | (child0 + ((order >> (2 * lane)) & 3u));
+          }
+          sp += __popc(rest);
+          __syncwarp();
+          lvl = lvl + 1;
+          G = child0 + ((order >> (2 * tf)) & 3u);
+          continue;
+        }
+        // best-first: keys are the leading lane's box distances; descend into
+        // the nearest child unless a queued node is nearer still
+        const float k0 = __shfl_sync(FULL, m0, leader), k1 = __shfl_sync(FULL, m1, leader);
+        const float k2 = __shfl_sync(FULL, m2, leader), k3 = __shfl_sync(FULL, m3, leader);
+        const int cf = (int)((order >> (2 * tf)) & 3u);
+        const float kf = cf == 0 ? k0 : cf == 1 ? k1 : cf == 2 ? k2 : k3;
+        const bool down = qn == 0 || kf <= __shfl_sync(FULL, qkey, 0);
+        const unsigned topush = down ? rest : om;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (!((topush >> t) & 1u)) continue;
+          const int c = (int)((order >> (2 * t)) & 3u);
+          qpush(c == 0 ? k0 : c == 1 ? k1 : c == 2 ? k2 : k3, lcode | (child0 + (uint32_t)c));
+        }
+        if (sp > PSTACK) return false;
+        __syncwarp();
+        if (down) {
+          lvl = lvl + 1;
+          G = child0 + (uint32_t)cf;
+          continue;
+        }
+      }
+    }
+    bool found = false;
+    __syncwarp();
+    while (true) {
+      uint32_t code;
+      if (sp > 0) {
+        --sp;
+        code = ps.code[sp];
+      } else if (qn > 0) {
+        code = __shfl_sync(FULL, qcode, 0);
+        qkey = __shfl_down_sync(FULL, qkey, 1);
+        qcode = __shfl_down_sync(FULL, qcode, 1);
+        --qn;
+      } else if (osp > 0) {
+        --osp;
+        code = ps.over[osp];
+      } else {
+        break;
+      }
       const int plvl = (int)(code >> 28);
       const uint32_t pG = code & 0x0fffffffu;
       // the node's box: lane (pG - 1) & 3 of its parent's group (pG - 1) >> 2

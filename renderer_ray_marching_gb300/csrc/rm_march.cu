@@ -104,7 +104,7 @@ enum { C_STEPS, C_RAYS, C_HITS, C_BAD, C_COOP, C_SOLO, C_LEAVES, C_NODES, C_WSTE
 // stepping loop does not hold lets more warps stay resident (the marcher is
 // bound by instruction latency, so resident warps are what hides it).
 struct WarpSmem {
-  PacketStack ps;
+  PacketQueue ps;
   ViewArgs v;                   // warp-uniform; written by lane 0 per item
   unsigned long long cnt[C_N];  // this warp's statistics
 };
@@ -199,7 +199,7 @@ __device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int t
 #pragma unroll 1
       for (int phase = 0; phase < (two ? 2 : 1); ++phase) {
         const bool part = phase == 0 ? tight : rest;
-        if (!packet_knn(ix, part, px, py, pz, L, sm.ps, lv, nd) && part) atomicAdd(sm.cnt + C_BAD, 1ull);
+        if (!packet_knn_bf(ix, part, px, py, pz, L, sm.ps, lv, nd) && part) atomicAdd(sm.cnt + C_BAD, 1ull);
       }
       if (two && lane == 0) sm.cnt[C_SPLIT] += 1;
       const unsigned any_step = __ballot_sync(FULL, stepping);  // every lane votes
