@@ -104,7 +104,7 @@ struct Ctx {
   DevBuf frame_bufs;     // device outputs for host-side frames
   DevBuf queue;          // work-queue counters
 
-  rm_launch launch{8, 4, 1, 6, 1};
+  rm_launch launch{8, 4, 1, 5, 1};
   rm_stats stats{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
