@@ -626,7 +626,8 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
   const int leader = __ffs(central ? central : act) - 1;
   const uint32_t last_first = (uint32_t)group_offset(ix.depth - 1);  // first group of level depth-1
   const unsigned long long qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
-  int sp = 0;     // depth-first stack (ps.code), used once `dfs` is set
+  int sp = 0;     // depth-first stack (ps.code from the bottom), used once `dfs` is set
+  int fsp = 0;    // far entries spilled at the switch (ps.code from the top), taken last
   int osp = 0;    // overflow stack (ps.over)
   int qn = 0;     // register queue: lane i holds the i-th nearest pending node
   float qkey = INF;
@@ -634,15 +635,19 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
   bool dfs = false;
   // queue insert (warp-uniform key and code); the farthest entry of a full
   // queue moves to the overflow stack, and a full overflow stack switches
-  // the walk to depth-first mode on the bounded stack
+  // the walk to depth-first mode on the bounded stack.  Entries spilled in
+  // the switching expansion (at most four: no queue insert happens after
+  // the switch) wait at the top of that stack and are taken last, after
+  // the queue and the overflow, so that far subtrees are not walked while
+  // the bounds are still loose.
   auto spill = [&](uint32_t code) {
     if (!dfs && osp < PKT_OVERFLOW) {
       if (lane == 0) ps.over[osp] = code;
       ++osp;
     } else {
       dfs = true;
-      if (sp < PSTACK && lane == 0) ps.code[sp] = code;
-      ++sp;
+      if (sp + fsp < PSTACK && lane == 0) ps.code[PSTACK - 1 - fsp] = code;
+      ++fsp;
     }
   };
   auto qpush = [&](float key, uint32_t code) {
@@ -739,7 +744,7 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
         if (dfs) {
           // depth-first: descend into the nearest needed child; lanes 0-3
           // push the others, farthest deepest so the nearest pops first
-          if (sp + 3 > PSTACK) return false;
+          if (sp + fsp + 3 > PSTACK) return false;
           if (lane < 4 && ((rest >> lane) & 1u)) {
             const int slot = sp + __popc(rest >> (lane + 1));
             ps.code[slot] = lcode | (child0 + ((order >> (2 * lane)) & 3u));
@@ -764,7 +769,7 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
           const int c = (int)((order >> (2 * t)) & 3u);
           qpush(c == 0 ? k0 : c == 1 ? k1 : c == 2 ? k2 : k3, lcode | (child0 + (uint32_t)c));
         }
-        if (sp > PSTACK) return false;
+        if (sp + fsp > PSTACK) return false;
         __syncwarp();
         if (down) {
           lvl = lvl + 1;
@@ -788,6 +793,9 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
       } else if (osp > 0) {
         --osp;
         code = ps.over[osp];
+      } else if (fsp > 0) {
+        --fsp;
+        code = ps.code[PSTACK - 1 - fsp];
       } else {
         break;
       }
