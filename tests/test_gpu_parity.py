@@ -258,3 +258,35 @@ def test_pinned_host_frames_equal_device_frames(scene100k):
             for name in ("rgbd", "depth"):
                 assert np.array_equal(a[name].view(np.int32), b[name].view(np.int32)), (key, name)
     r.close()
+
+
+@pytest.mark.parametrize("search", [1, 0])
+def test_render_with_duplicate_points_matches_oracle(search):
+    """40% of the points are exact copies of others, so equal distances are
+    everywhere: the neighbour set's ordered path (ties by cloud index,
+    duplicates skipped) and the tie pass of its re-sort both run."""
+    sc = syn.make_scene(60_000, n_boxes=8, seed=11)
+    xyz = sc.xyz.copy()
+    rng = np.random.default_rng(5)
+    dst = rng.choice(xyz.shape[0], xyz.shape[0] * 2 // 5, replace=False)
+    xyz[dst] = xyz[rng.integers(0, xyz.shape[0], dst.shape[0])]
+    r, radii, nn = make_renderer(xyz, sc.rgb, search=search)
+    ix = oracle.Index(xyz)
+    orad, onn = ix.radii(0.0)
+    assert np.array_equal(radii.view(np.int32), orad.view(np.int32))
+    assert np.array_equal(nn, onn)
+    assert (radii == 0).mean() > 0.2  # duplicates have a zero radius
+    rc = np.minimum(radii, np.float32(0.1))
+    views = views_from_specs(syn.make_views(2, seed=6, boxes=sc.boxes, resolutions=[(160, 120), (96, 64)]))
+    batch = r.render_batch(views, outputs=("hit", "depth", "steps"), device=False)
+    for v, b in zip(views, batch):
+        plain = r.render(v, outputs=("hit", "depth", "steps"))
+        oh, od, os_ = ix.render(rc, oracle_view(r, v))
+        for out in (plain, b):
+            gh, gd, gs = out["hit"].reshape(-1), out["depth"].reshape(-1), out["steps"].reshape(-1)
+            assert np.array_equal(gh, oh)
+            assert np.array_equal(gd.view(np.int32), od.view(np.int32))
+            assert np.array_equal(gs[oh >= 0], os_[oh >= 0]) and np.all(gs[oh < 0] <= os_[oh < 0])
+        assert (oh >= 0).mean() > 0.5
+    assert r.stats()["search_errors"] == 0
+    r.close()
