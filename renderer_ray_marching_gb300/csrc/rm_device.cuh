@@ -160,11 +160,6 @@ __device__ __forceinline__ void klist_insert(KList<K>& L, float d, int32_t s, fl
   }
 }
 
-template <int K>
-__device__ __forceinline__ float klist_worst(const KList<K>& L) {
-  return L.d[K - 1];
-}
-
 // The marcher's 10 nearest, kept sorted by (d2, cloud index) in registers
 // (empty slots (+inf, -1) last), so the bound is always d[KNN-1].
 // Insertions skip points already present, so the set can start from the
