@@ -349,6 +349,22 @@ def main():
         value = ws * total_rays / (t_step * 1e-3) / 1e6
         hits_total = int(sum(int((h >= 0).sum().item()) for _, h in keep))
 
+        # ---- the same batch with one independent tree walk per ray (the
+        # reference's execution model) instead of the warp packet walk
+        per_ray = None
+        if not args.skip_plain:
+            L0 = r.get_launch()
+            r.set_launch(L0["tile_w"], L0["tile_h"], 1, 4, 0)
+            r.render_batch_into(views, frames, device=True, cviews=cviews)
+            r.synchronize()
+            e0.record(stream)
+            r.render_batch_into(views, frames, device=True, cviews=cviews)
+            e1.record(stream)
+            e1.synchronize()
+            per_ray = total_rays / (e0.elapsed_time(e1) * 1e-3) / 1e6
+            r.set_launch(L0["tile_w"], L0["tile_h"], L0["rays_per_lane"], L0["ctas_per_sm"], L0["search"])
+            log("per-ray walk %.2f Mrays/s" % per_ray)
+
         # ---- plain per-view form, same views
         plain, plain_ms = None, None
         if not args.skip_plain:
@@ -407,6 +423,7 @@ def main():
                       "l2": "inputs larger than L2 (cloud + index >= 0.8 GB), no flush",
                       "launch": tune, "parallelism": "replicas" if ws > 1 else "single"},
            "plain_mrays_s": None if plain is None else round(plain, 3),
+           "per_ray_walk_mrays_s": None if per_ray is None else round(per_ray, 3),
            "batched_over_plain": None if plain is None else round(value / ws / plain, 3),
            "radii_mqueries_s": round(radii_mq, 3), "radii_ms": round(float(np.median(radii_ms)), 3),
            "radii_build_ms": round(float(np.median(build_ms)), 3), "radii_query_ms": round(float(np.median(query_ms)), 3),
