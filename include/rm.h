@@ -95,7 +95,8 @@ typedef struct {
   int64_t packet_leaves; /* leaves scanned by packet traversals */
   int64_t packet_nodes;  /* tree nodes expanded by packet traversals */
   int64_t warp_steps;    /* warp-wide distance steps */
-  int64_t split_steps;   /* warp steps whose lanes were split into two packets */
+  int64_t split_steps;   /* warp steps whose lanes were split into two packets (the best-first
+                            walk does not split; kept for layout, always 0) */
   int64_t search_errors; /* searches that hit a self-check bound (0 unless the index is broken) */
   float kernel_ms;       /* device time of the last render launch (graph for the batch) */
 } rm_stats;

@@ -96,6 +96,7 @@ struct ViewArgs {
 // counters: [0] steps, [1] rays, [2] hits, [3] search errors,
 //           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets,
 //           [7] nodes expanded by packets, [8] warp steps, [9] warp steps split in two packets
+//           (no longer split: always 0)
 enum { C_STEPS, C_RAYS, C_HITS, C_BAD, C_COOP, C_SOLO, C_LEAVES, C_NODES, C_WSTEPS, C_SPLIT, C_N };
 
 // Per-warp shared state.  The view of the current item and the statistics
@@ -108,12 +109,6 @@ struct WarpSmem {
   ViewArgs v;                   // warp-uniform; written by lane 0 per item
   unsigned long long cnt[C_N];  // this warp's statistics
 };
-
-__device__ __forceinline__ float warp_min(float v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, off));
-  return v;
-}
 
 __device__ __forceinline__ void write_result(const IndexDev& ix, const ViewArgs& v, int64_t pix, int32_t s,
                                              float depth, int32_t steps, unsigned long long* cnt) {
@@ -185,23 +180,12 @@ __device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int t
     float pz = __fmaf_rn(r.dz, t, r.oz);
     if (stepping) L.rewarm(ix, px, py, pz);
     if (SEARCH == 1) {
-      // Two packets at most: lanes whose bound is within 8x (in radius; 64x in d2) of the
-      // tightest lane's, then the rest (rays just started or still far from
-      // every surface).  One loose lane would otherwise make the whole warp
-      // walk everything inside its ball.
-      float bmin = warp_min(stepping ? L.worst() : INFINITY);
-      bool tight = stepping && L.worst() <= 64.0f * bmin;
+      // One packet: every stepping lane walks with the warp.  (A split into
+      // a tight and a loose packet helped the depth-first walk; with the
+      // best-first order loose lanes no longer steer the walk and the split
+      // measured 2% slower.)
       unsigned lv = 0, nd = 0;
-      const bool rest = stepping && !tight;
-      const bool two = __ballot_sync(FULL, rest) != 0;
-      // one call site for both packets: the walk is large, and a second
-      // inlined copy costs more in instruction fetch than the loop does
-#pragma unroll 1
-      for (int phase = 0; phase < (two ? 2 : 1); ++phase) {
-        const bool part = phase == 0 ? tight : rest;
-        if (!packet_knn_bf(ix, part, px, py, pz, L, sm.ps, lv, nd) && part) atomicAdd(sm.cnt + C_BAD, 1ull);
-      }
-      if (two && lane == 0) sm.cnt[C_SPLIT] += 1;
+      if (!packet_knn_bf(ix, stepping, px, py, pz, L, sm.ps, lv, nd) && stepping) atomicAdd(sm.cnt + C_BAD, 1ull);
       const unsigned any_step = __ballot_sync(FULL, stepping);  // every lane votes
       if (lane == 0) {
         sm.cnt[C_LEAVES] += lv;
