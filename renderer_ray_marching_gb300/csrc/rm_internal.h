@@ -68,8 +68,7 @@ struct ViewDev {
   int32_t tiles_x;      // warp tiles across
   int32_t tiles_y;
   int64_t tile_base;    // first work item of this view
-  float t_clip;         // culling: rays beyond this t cannot hit (see culling kernel)
-  float pad0;
+  float reserved[2];    // keeps the 136-byte layout the allocation-free scratch is sized for
   float4* rgbd;
   int32_t* hit;
   float* depth;
@@ -110,7 +109,6 @@ struct Ctx {
 
   // cached CUDA graph of the batched launch
   cudaGraphExec_t graph_exec = nullptr;
-  std::vector<ViewDev> graph_views;
   void* graph_key_views = nullptr;
   int graph_key_n = -1;
   rm_launch graph_key_launch{0, 0, 0, 0, 0};
