@@ -184,6 +184,19 @@ def traffic_per_ray():
     return None
 
 
+def hit_checksum(keep) -> int:
+    """Order-sensitive 64-bit checksum of every view's hit map (full-size
+    property checks: the same batch through another path must give the same
+    hit indices)."""
+    import torch
+    total = 0
+    for i, (_, h) in enumerate(keep):
+        flat = h.reshape(-1).to(torch.int64)
+        w = torch.arange(1, flat.numel() + 1, device=flat.device, dtype=torch.int64) * (2 * i + 1)
+        total = (total * 1000003 + int(((flat + 2) * w).sum().item())) & 0xFFFFFFFFFFFFFFFF
+    return total
+
+
 def cpu_sample_render(sc, views, radii_clamped, n_rays, seed, threads=0):
     """Oracle (the reference marcher loop restated in C, exact 10-NN) on a
     bounded, seeded sample of rays spread over the views.  Returns
@@ -348,6 +361,8 @@ def main():
             t_step = float(tt.item())
         value = ws * total_rays / (t_step * 1e-3) / 1e6
         hits_total = int(sum(int((h >= 0).sum().item()) for _, h in keep))
+        hit_sum = hit_checksum(keep)
+        checks = {}
 
         # ---- the same batch with one independent tree walk per ray (the
         # reference's execution model) instead of the warp packet walk
@@ -362,6 +377,7 @@ def main():
             e1.record(stream)
             e1.synchronize()
             per_ray = total_rays / (e0.elapsed_time(e1) * 1e-3) / 1e6
+            checks["per_ray_equals_packet"] = hit_checksum(keep) == hit_sum
             r.set_launch(L0["tile_w"], L0["tile_h"], L0["rays_per_lane"], L0["ctas_per_sm"], L0["search"])
             log("per-ray walk %.2f Mrays/s" % per_ray)
 
@@ -375,6 +391,7 @@ def main():
             e1.record(stream)
             e1.synchronize()
             plain_ms = e0.elapsed_time(e1)
+            checks["plain_equals_batched"] = hit_checksum(keep) == hit_sum
             plain = total_rays / (plain_ms * 1e-3) / 1e6
         log("timed batch %.1f ms/step, plain %s ms" % (t_step, plain_ms))
 
@@ -430,6 +447,7 @@ def main():
            "fwd_ms_per_view": fb["fwd_ms"], "fwdbwd_ms_per_view": fb["fwdbwd_ms"],
            "fwdbwd_over_fwd": fb["ratio"],
            "steps_per_ray": round(steps_total / total_rays, 3), "hit_fraction": round(hits_total / total_rays, 4),
+           "checks": checks,
            "e2e": {"value": None if e2e is None else round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
            "roofline": {"bound": "hbm", "kernel": "k_march_batch", "achieved": round(achieved, 1), "peak": peak,
