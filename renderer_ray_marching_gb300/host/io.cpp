@@ -282,7 +282,8 @@ void write_radii_archive(const std::string& path, const std::vector<float>& radi
   fprintf(f, "22 serialization::archive 17 0 0 %zu 0", radii.size());
   for (float r : radii) fprintf(f, " %.9e", (double)r);
   fputc('\n', f);
-  if (fclose(f) != 0) throw std::runtime_error("cannot write radii file " + path);
+  const bool bad = ferror(f) != 0;  // a short write (e.g. a full disk) must not pass silently
+  if (fclose(f) != 0 || bad) throw std::runtime_error("cannot write radii file " + path);
 }
 
 // ------------------------------------------------------------------ JSON
@@ -458,7 +459,7 @@ void write_png(const std::string& path, int width, int height, int channels, con
     if (f) fclose(f);
     throw std::runtime_error("cannot write " + path);
   }
-  fclose(f);
+  if (fclose(f) != 0) throw std::runtime_error("cannot write " + path);
 }
 
 void write_npy_f32(const std::string& path, int height, int width, const float* data) {
@@ -487,7 +488,8 @@ void write_npy_f32(const std::string& path, int height, int width, const float* 
   } else {
     fwrite(data, 4, n, f);
   }
-  if (fclose(f) != 0) throw std::runtime_error("cannot write " + path);
+  const bool bad = ferror(f) != 0;  // a short write (e.g. a full disk) must not pass silently
+  if (fclose(f) != 0 || bad) throw std::runtime_error("cannot write " + path);
 }
 
 void encode_colour_rgba8(int width, int height, const float* rgbd, std::vector<uint8_t>& out) {
