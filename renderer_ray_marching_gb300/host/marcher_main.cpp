@@ -97,6 +97,9 @@ void check(rm_ctx* ctx, rm_status s, const char* what) {
 // Advisory POSIX record lock on the whole file, held while the fd is open.
 struct FileLock {
   int fd = -1;
+  FileLock() = default;
+  FileLock(const FileLock&) = delete;  // one owner per descriptor
+  FileLock& operator=(const FileLock&) = delete;
   bool try_lock(const fs::path& p) {
     fd = ::open(p.c_str(), O_RDWR | O_CREAT, 0644);
     if (fd < 0) return false;
