@@ -104,3 +104,13 @@ def test_json_rows_become_columns():
     assert np.array_equal(m.reshape(4, 4).T, np.arange(1, 17, dtype=np.float32).reshape(4, 4))
     with pytest.raises(RuntimeError):
         fileio.json_mat4("[[1,2],[3]]")
+
+
+def test_writers_report_unwritable_paths(tmp_path):
+    """A writer that cannot create its file raises instead of passing silently."""
+    missing = tmp_path / "no" / "such" / "dir"
+    with pytest.raises(RuntimeError, match="cannot write"):
+        fileio.write_radii(str(missing / "a.radii"), np.ones(4, np.float32))
+    rgbd = np.zeros((3, 5, 4), np.float32)
+    with pytest.raises(RuntimeError, match="cannot write"):
+        fileio.write_frame(str(missing / "c.png"), str(missing / "c_depth.png"), rgbd)
