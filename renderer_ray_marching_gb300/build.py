@@ -67,8 +67,8 @@ def build_host() -> None:
     """librm_io.so (file formats, no CUDA) and marcher.bin (links both libraries)."""
     io_srcs = [os.path.join(HOST, "io.cpp"), os.path.join(HOST, "rmio_c.cpp")]
     tmp = IOLIB + ".tmp%d" % os.getpid()
-    cmd = (["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I" + INCLUDE, "-I" + HOST,
-            "-o", tmp] + io_srcs + ["-lz"])
+    cmd = (["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", "-I" + INCLUDE,
+            "-I" + HOST, "-o", tmp] + io_srcs + ["-lz"])
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("io library build failed:\n%s\n%s" % (" ".join(cmd), r.stderr[-4000:]))

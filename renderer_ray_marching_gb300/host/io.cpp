@@ -9,9 +9,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <fstream>
+#include <iterator>
 #include <sstream>
 #include <stdexcept>
+#include <thread>
 
 namespace rmio {
 
@@ -243,44 +246,132 @@ void save_ply(const std::string& path, const Cloud& c) {
 }
 
 // ------------------------------------------------------------------ radii archive
+namespace {
+
+// Worker count for the archive's per-value formatting and parsing: at 10^8
+// points the text archive, not the GPU radii, is what a radii-cache run
+// waits for (tens of seconds single-threaded).
+unsigned archive_threads(size_t work) {
+  if (work < ((size_t)1 << 20)) return 1;
+  unsigned t = std::thread::hardware_concurrency();
+  if (t == 0) t = 4;
+  return std::min(t, 32u);
+}
+
+// f(slice, begin, end) over nt contiguous slices of [0, n), on nt threads;
+// the first exception thrown by a slice is rethrown here.
+template <class F>
+void parallel_slices(size_t n, unsigned nt, F&& f) {
+  if (nt <= 1) {
+    f(0u, (size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  std::vector<std::exception_ptr> err(nt);
+  for (unsigned c = 0; c < nt; ++c) {
+    const size_t b = n * c / nt, e = n * (c + 1) / nt;
+    th.emplace_back([&f, &err, c, b, e] {
+      try {
+        f(c, b, e);
+      } catch (...) {
+        err[c] = std::current_exception();
+      }
+    });
+  }
+  for (auto& t : th) t.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
+}
+
+inline bool is_space(char ch) { return std::isspace((unsigned char)ch) != 0; }
+
+}  // namespace
+
 std::vector<float> read_radii_archive(const std::string& path) {
-  std::ifstream f(path);
+  std::ifstream f(path, std::ios::binary);
   if (!f) throw std::runtime_error("cannot open radii file " + path);
+  std::string data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  const size_t size = data.size();
+  size_t pos = 0;
+  auto next_token = [&](std::string* out) -> bool {
+    while (pos < size && is_space(data[pos])) ++pos;
+    if (pos >= size) return false;
+    const size_t b = pos;
+    while (pos < size && !is_space(data[pos])) ++pos;
+    if (out) out->assign(data, b, pos - b);
+    return true;
+  };
   std::string t0, t1, ver;
-  f >> t0 >> t1 >> ver;
-  if (t0 != "22" || t1 != "serialization::archive")
+  if (!next_token(&t0) || !next_token(&t1) || !next_token(&ver) || t0 != "22" ||
+      t1 != "serialization::archive")
     throw std::runtime_error("radii file " + path + " is not a Boost text archive");
-  std::vector<std::string> tok;
-  std::string s;
-  while (f >> s) tok.push_back(s);
+  const size_t body = pos;
+  // token starts per slice of the body (a token starts at a non-space byte
+  // that follows a space), then their prefix sums: global token numbers
+  const unsigned nt = archive_threads(size - body);
+  std::vector<size_t> count(nt, 0), first(nt + 1, 0);
+  auto starts_token = [&](size_t i) { return !is_space(data[i]) && (i == body || is_space(data[i - 1])); };
+  parallel_slices(size - body, nt, [&](unsigned c, size_t b, size_t e) {
+    size_t k = 0;
+    for (size_t i = body + b; i < body + e; ++i) k += starts_token(i) ? 1 : 0;
+    count[c] = k;
+  });
+  for (unsigned c = 0; c < nt; ++c) first[c + 1] = first[c] + count[c];
+  const size_t ntok = first[nt];
+  std::vector<std::string> head;  // up to four leading tokens, for the layout
+  for (std::string t; head.size() < 4 && next_token(&t);) head.push_back(t);
   auto is_uint = [](const std::string& x) {
     return !x.empty() && std::all_of(x.begin(), x.end(), [](char ch) { return std::isdigit((unsigned char)ch); });
   };
   // candidate layouts: (leading tokens before count, tokens after count)
   const int layouts[4][2] = {{2, 1}, {2, 0}, {0, 1}, {0, 0}};
   for (auto& L : layouts) {
-    size_t lead = L[0], after = L[1];
-    if (tok.size() < lead + 1 + after) continue;
-    if (!is_uint(tok[lead])) continue;
-    size_t count = std::stoull(tok[lead]);
-    if (tok.size() != lead + 1 + after + count) continue;
-    std::vector<float> out(count);
-    for (size_t i = 0; i < count; ++i) {
-      const std::string& v = tok[lead + 1 + after + i];
-      char* end = nullptr;
-      out[i] = std::strtof(v.c_str(), &end);
-      if (end == v.c_str()) throw std::runtime_error("radii file " + path + ": bad value '" + v + "'");
-    }
+    const size_t lead = L[0], after = L[1];
+    if (ntok < lead + 1 + after || head.size() <= lead || !is_uint(head[lead])) continue;
+    const size_t n = std::stoull(head[lead]);
+    if (ntok != lead + 1 + after + n) continue;
+    const size_t vstart = lead + 1 + after;  // token number of the first value
+    std::vector<float> out(n);
+    parallel_slices(size - body, nt, [&](unsigned c, size_t b, size_t e) {
+      size_t g = first[c];
+      for (size_t i = body + b; i < body + e; ++i) {
+        if (!starts_token(i)) continue;
+        if (g >= vstart) {
+          char* end = nullptr;
+          out[g - vstart] = std::strtof(data.c_str() + i, &end);
+          if (end == data.c_str() + i) {
+            size_t j = i;
+            while (j < size && !is_space(data[j])) ++j;
+            throw std::runtime_error("radii file " + path + ": bad value '" + data.substr(i, j - i) + "'");
+          }
+        }
+        ++g;
+      }
+    });
     return out;
   }
   throw std::runtime_error("radii file " + path + ": element count does not match its contents");
 }
 
 void write_radii_archive(const std::string& path, const std::vector<float>& radii) {
+  // values are formatted in parallel slices and written in order: the bytes
+  // equal those of one fprintf(" %.9e") per value
+  const size_t n = radii.size();
+  const unsigned nt = archive_threads(n);
+  std::vector<std::string> parts(nt);
+  parallel_slices(n, nt, [&](unsigned c, size_t b, size_t e) {
+    std::string& out = parts[c];
+    out.reserve((e - b) * 17);
+    char buf[48];
+    for (size_t i = b; i < e; ++i) {
+      const int k = snprintf(buf, sizeof(buf), " %.9e", (double)radii[i]);
+      out.append(buf, (size_t)k);
+    }
+  });
   FILE* f = fopen(path.c_str(), "w");
   if (!f) throw std::runtime_error("cannot write radii file " + path);
-  fprintf(f, "22 serialization::archive 17 0 0 %zu 0", radii.size());
-  for (float r : radii) fprintf(f, " %.9e", (double)r);
+  fprintf(f, "22 serialization::archive 17 0 0 %zu 0", n);
+  for (const std::string& part : parts) fwrite(part.data(), 1, part.size(), f);
   fputc('\n', f);
   const bool bad = ferror(f) != 0;  // a short write (e.g. a full disk) must not pass silently
   if (fclose(f) != 0 || bad) throw std::runtime_error("cannot write radii file " + path);

@@ -114,3 +114,26 @@ def test_writers_report_unwritable_paths(tmp_path):
     rgbd = np.zeros((3, 5, 4), np.float32)
     with pytest.raises(RuntimeError, match="cannot write"):
         fileio.write_frame(str(missing / "c.png"), str(missing / "c_depth.png"), rgbd)
+
+
+def test_radii_archive_parallel_paths_are_exact(tmp_path):
+    """Above about 10^6 values the archive is written and parsed in parallel
+    slices: the bytes must equal one ' %.9e' per value in order, and any of
+    the accepted layouts must parse back exactly."""
+    rng = np.random.default_rng(3)
+    r = (rng.random(1_200_000) * 0.1).astype(np.float32)
+    r[::997] = 0.0
+    p = tmp_path / "big.radii"
+    fileio.write_radii(str(p), r)
+    text = "22 serialization::archive 17 0 0 %d 0" % r.size + "".join(" %.9e" % v for v in r.tolist()) + "\n"
+    assert p.read_text() == text
+    assert np.array_equal(fileio.read_radii(str(p)).view(np.int32), r.view(np.int32))
+    # layout without class information or item version, values split over lines
+    body = "22 serialization::archive 17 %d" % r.size + "".join(
+        ("\n" if i % 1000 == 0 else " ") + ("%.9e" % v) for i, v in enumerate(r.tolist()))
+    q = tmp_path / "plain.radii"
+    q.write_text(body)
+    assert np.array_equal(fileio.read_radii(str(q)).view(np.int32), r.view(np.int32))
+    q.write_text(body.replace(" 1.", " x.", 1))
+    with pytest.raises(RuntimeError, match="bad value"):
+        fileio.read_radii(str(q))
