@@ -21,6 +21,48 @@ namespace rmio {
 // ------------------------------------------------------------------ PLY
 namespace {
 
+// Worker count for host-side per-point loops (PLY decoding, the radii
+// archive's formatting and parsing): at 10^8 points these, not the GPU
+// kernels, are what a CLI run waits for (seconds to tens of seconds on one
+// thread).  Small inputs stay on the calling thread.
+unsigned host_threads(size_t work) {
+  if (work < ((size_t)1 << 20)) return 1;
+  unsigned t = std::thread::hardware_concurrency();
+  if (t == 0) t = 4;
+  return std::min(t, 32u);
+}
+
+// f(slice, begin, end) over nt contiguous slices of [0, n), on nt threads;
+// the first exception thrown by a slice is rethrown here.
+template <class F>
+void parallel_slices(size_t n, unsigned nt, F&& f) {
+  if (nt <= 1) {
+    f(0u, (size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  std::vector<std::exception_ptr> err(nt);
+  for (unsigned c = 0; c < nt; ++c) {
+    const size_t b = n * c / nt, e = n * (c + 1) / nt;
+    th.emplace_back([&f, &err, c, b, e] {
+      try {
+        f(c, b, e);
+      } catch (...) {
+        err[c] = std::current_exception();
+      }
+    });
+  }
+  for (auto& t : th) t.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
+}
+
+inline bool is_space(char ch) { return std::isspace((unsigned char)ch) != 0; }
+
+}  // namespace
+
+namespace {
+
 enum class PType { I8, U8, I16, U16, I32, U32, F32, F64 };
 
 PType parse_ptype(const std::string& t) {
@@ -186,25 +228,30 @@ Cloud load_ply(const std::string& path) {
         }
       }
     } else if (!has_list) {
-      std::vector<unsigned char> buf(stride * std::min<size_t>(e.count, 1 << 16));
+      // fixed-size records: read in chunks of up to 4M records, decode each
+      // chunk in parallel slices
+      const size_t chunk = (size_t)1 << 22;
+      std::vector<unsigned char> buf(stride * std::min<size_t>(e.count, chunk));
       size_t done = 0;
       while (done < e.count) {
-        size_t m = std::min<size_t>(e.count - done, 1 << 16);
+        size_t m = std::min<size_t>(e.count - done, chunk);
         f.read((char*)buf.data(), (std::streamsize)(stride * m));
         if ((size_t)f.gcount() != stride * m) throw std::runtime_error("PLY: truncated " + path);
         if (is_vertex) {
-          for (size_t j = 0; j < m; ++j) {
-            const unsigned char* r = buf.data() + j * stride;
-            size_t i = done + j;
-            c.xyz[3 * i + 0] = (float)read_bin(r + off[ix], e.props[ix].type, swap);
-            c.xyz[3 * i + 1] = (float)read_bin(r + off[iy], e.props[iy].type, swap);
-            c.xyz[3 * i + 2] = (float)read_bin(r + off[iz], e.props[iz].type, swap);
-            if (colour) {
-              c.rgb[3 * i + 0] = to_u8(read_bin(r + off[ir], e.props[ir].type, swap), e.props[ir].type);
-              c.rgb[3 * i + 1] = to_u8(read_bin(r + off[ig], e.props[ig].type, swap), e.props[ig].type);
-              c.rgb[3 * i + 2] = to_u8(read_bin(r + off[ib], e.props[ib].type, swap), e.props[ib].type);
+          parallel_slices(m, host_threads(m), [&](unsigned, size_t jb, size_t je) {
+            for (size_t j = jb; j < je; ++j) {
+              const unsigned char* r = buf.data() + j * stride;
+              size_t i = done + j;
+              c.xyz[3 * i + 0] = (float)read_bin(r + off[ix], e.props[ix].type, swap);
+              c.xyz[3 * i + 1] = (float)read_bin(r + off[iy], e.props[iy].type, swap);
+              c.xyz[3 * i + 2] = (float)read_bin(r + off[iz], e.props[iz].type, swap);
+              if (colour) {
+                c.rgb[3 * i + 0] = to_u8(read_bin(r + off[ir], e.props[ir].type, swap), e.props[ir].type);
+                c.rgb[3 * i + 1] = to_u8(read_bin(r + off[ig], e.props[ig].type, swap), e.props[ig].type);
+                c.rgb[3 * i + 2] = to_u8(read_bin(r + off[ib], e.props[ib].type, swap), e.props[ib].type);
+              }
             }
-          }
+          });
         }
         done += m;
       }
@@ -246,46 +293,6 @@ void save_ply(const std::string& path, const Cloud& c) {
 }
 
 // ------------------------------------------------------------------ radii archive
-namespace {
-
-// Worker count for the archive's per-value formatting and parsing: at 10^8
-// points the text archive, not the GPU radii, is what a radii-cache run
-// waits for (tens of seconds single-threaded).
-unsigned archive_threads(size_t work) {
-  if (work < ((size_t)1 << 20)) return 1;
-  unsigned t = std::thread::hardware_concurrency();
-  if (t == 0) t = 4;
-  return std::min(t, 32u);
-}
-
-// f(slice, begin, end) over nt contiguous slices of [0, n), on nt threads;
-// the first exception thrown by a slice is rethrown here.
-template <class F>
-void parallel_slices(size_t n, unsigned nt, F&& f) {
-  if (nt <= 1) {
-    f(0u, (size_t)0, n);
-    return;
-  }
-  std::vector<std::thread> th;
-  std::vector<std::exception_ptr> err(nt);
-  for (unsigned c = 0; c < nt; ++c) {
-    const size_t b = n * c / nt, e = n * (c + 1) / nt;
-    th.emplace_back([&f, &err, c, b, e] {
-      try {
-        f(c, b, e);
-      } catch (...) {
-        err[c] = std::current_exception();
-      }
-    });
-  }
-  for (auto& t : th) t.join();
-  for (auto& e : err)
-    if (e) std::rethrow_exception(e);
-}
-
-inline bool is_space(char ch) { return std::isspace((unsigned char)ch) != 0; }
-
-}  // namespace
 
 std::vector<float> read_radii_archive(const std::string& path) {
   std::ifstream f(path, std::ios::binary);
@@ -308,7 +315,7 @@ std::vector<float> read_radii_archive(const std::string& path) {
   const size_t body = pos;
   // token starts per slice of the body (a token starts at a non-space byte
   // that follows a space), then their prefix sums: global token numbers
-  const unsigned nt = archive_threads(size - body);
+  const unsigned nt = host_threads(size - body);
   std::vector<size_t> count(nt, 0), first(nt + 1, 0);
   auto starts_token = [&](size_t i) { return !is_space(data[i]) && (i == body || is_space(data[i - 1])); };
   parallel_slices(size - body, nt, [&](unsigned c, size_t b, size_t e) {
@@ -357,7 +364,7 @@ void write_radii_archive(const std::string& path, const std::vector<float>& radi
   // values are formatted in parallel slices and written in order: the bytes
   // equal those of one fprintf(" %.9e") per value
   const size_t n = radii.size();
-  const unsigned nt = archive_threads(n);
+  const unsigned nt = host_threads(n);
   std::vector<std::string> parts(nt);
   parallel_slices(n, nt, [&](unsigned c, size_t b, size_t e) {
     std::string& out = parts[c];

@@ -137,3 +137,27 @@ def test_radii_archive_parallel_paths_are_exact(tmp_path):
     q.write_text(body.replace(" 1.", " x.", 1))
     with pytest.raises(RuntimeError, match="bad value"):
         fileio.read_radii(str(q))
+
+
+@pytest.mark.parametrize("order", ["<", ">"])
+def test_ply_parallel_decode_large(tmp_path, order):
+    """Above about 10^6 vertices the binary records are decoded in parallel
+    slices; both byte orders and mixed property types must come out exact."""
+    n = 1_200_000
+    rng = np.random.default_rng(7)
+    dt = np.dtype([("x", order + "f8"), ("y", order + "f4"), ("z", order + "f4"), ("nx", order + "f4"),
+                   ("red", "u1"), ("green", "u1"), ("blue", "u1")])
+    rec = np.zeros(n, dt)
+    for k in ("x", "y", "z", "nx"):
+        rec[k] = rng.normal(size=n)
+    for k in ("red", "green", "blue"):
+        rec[k] = rng.integers(0, 256, n)
+    fmt = "binary_little_endian" if order == "<" else "binary_big_endian"
+    header = ("ply\nformat %s 1.0\nelement vertex %d\nproperty double x\nproperty float y\nproperty float z\n"
+              "property float nx\nproperty uchar red\nproperty uchar green\nproperty uchar blue\nend_header\n" % (fmt, n))
+    p = tmp_path / "big.ply"
+    p.write_bytes(header.encode() + rec.tobytes())
+    xyz, rgb = fileio.load_ply(str(p))
+    want = np.stack([rec["x"].astype(np.float32), rec["y"].astype(np.float32), rec["z"].astype(np.float32)], 1)
+    assert np.array_equal(xyz, want)
+    assert np.array_equal(rgb, np.stack([rec["red"], rec["green"], rec["blue"]], 1))
