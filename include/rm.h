@@ -169,10 +169,11 @@ rm_status rm_render_batch(rm_ctx* ctx, const rm_view* views, int32_t n, const rm
 rm_status rm_set_launch(rm_ctx* ctx, const rm_launch* launch);
 rm_status rm_get_launch(rm_ctx* ctx, rm_launch* launch);
 
-/* Autotuner: times candidate tile shapes, rays per lane and index leaf
- * sizes on the given views (device-resident scratch outputs) and keeps the
- * fastest.  Rebuilds the index when the leaf size changes.  `best_ms`
- * (may be NULL) receives the winning time. */
+/* Autotuner: times candidate tile shapes, CTAs per SM, search modes (with
+ * rays per lane for the per-ray walk) and index leaf sizes on the given
+ * views (device-resident scratch outputs) and keeps the fastest.  Rebuilds
+ * the index when the leaf size changes.  `best_ms` (may be NULL) receives
+ * the winning time. */
 rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* chosen,
                       int32_t* leaf_size, float* best_ms);
 
