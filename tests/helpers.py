@@ -72,7 +72,13 @@ def brute_march(xyz, radii, o, d, t_near, t_far, max_steps=128, min_dist=np.floa
     for i in range(max_steps):
         p = np.array([np.float32(fmaf(d[a], t, o[a])) for a in range(3)], np.float32)
         dd = d2_fast(xyz, p)
-        part = np.argpartition(dd, min(10, n - 1))[:min(10, n)] if n > 10 else idx
+        # the 10 nearest in (d2, index) order, exact under ties: every point
+        # tied with the 10th distance is a candidate before the final sort
+        if n > 10:
+            kth = np.partition(dd, 9)[9]
+            part = np.nonzero(dd <= kth)[0]
+        else:
+            part = idx
         order = part[np.lexsort((part, dd[part]))][:10]
         best, bi = np.float32(np.inf), 0
         for j in order:

@@ -97,3 +97,31 @@ def test_march_against_brute_force_rays():
         assert (hit[k], steps[k]) == (bh, bs), (k, p)
         assert np.float32(depth[k]).view(np.int32) == np.float32(bd).view(np.int32)
     assert (hit >= 0).mean() > 0.3
+
+
+def test_march_with_duplicate_points_against_brute_force():
+    """A cloud in which many points are exact copies (equal distances at
+    every step): the oracle's march keeps (d2, index) order and the strict
+    '<' of the step value exactly as the brute-force loop does."""
+    from renderer_ray_marching_gb300 import synthetic as syn
+    from tests.helpers import brute_march
+    sc = syn.make_scene(12000, n_boxes=6, seed=22)
+    xyz = sc.xyz.copy()
+    rng = np.random.default_rng(8)
+    dst = rng.choice(xyz.shape[0], xyz.shape[0] // 2, replace=False)
+    xyz[dst] = xyz[rng.integers(0, xyz.shape[0], dst.shape[0])]
+    ix = oracle.Index(xyz)
+    radii, _ = ix.radii(0.1)
+    assert (radii == 0).mean() > 0.3
+    spec = syn.make_views(1, seed=4, boxes=sc.boxes, resolutions=[(48, 32)])[0]
+    m, w, h, fov = syn.view_params(spec)
+    pane = np.float32(np.float32(w) / (np.float32(2.0) * np.float32(math.tan(np.float32(0.5) * fov))))
+    v = oracle.make_view(m, w, h, pane)
+    pix = np.random.default_rng(1).choice(w * h, 40, replace=False).astype(np.int64)
+    hit, depth, steps = ix.render(radii, v, pix)
+    for k, p in enumerate(pix):
+        o, d, tn, tf = oracle.ray(v, int(p % w), int(p // w))
+        bh, bd, bs = brute_march(xyz, radii, o, d, tn, tf)
+        assert (hit[k], steps[k]) == (bh, bs), (k, p)
+        assert np.float32(depth[k]).view(np.int32) == np.float32(bd).view(np.int32)
+    assert (hit >= 0).mean() > 0.3
