@@ -49,8 +49,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c4"],
                     help="c2: 20M points, 40 boxes, 256 mixed-resolution views (the headline); "
+                         "c1: 2M points, 12 boxes, max_radius 0.05, 64 views at 1067x690; "
                          "c4: 100M points, per-surface density log-uniform over 100x, 1024 views at 1067x690, "
                          "fwd+bwd on 64 of them")
     ap.add_argument("--points", type=int, default=None)
@@ -83,9 +84,10 @@ def dist_info():
 
 WORKLOADS = {
     # points, boxes, per-surface density range, views, resolutions (None: the
-    # reference's README intrinsics, 1067x690)
-    "c2": dict(points=20_000_000, boxes=40, density=1.0, views=256, res=RES),
-    "c4": dict(points=100_000_000, boxes=12, density=100.0, views=1024, res=None),
+    # reference's README intrinsics, 1067x690), max_radius (the -r flag)
+    "c1": dict(points=2_000_000, boxes=12, density=1.0, views=64, res=None, max_radius=0.05),
+    "c2": dict(points=20_000_000, boxes=40, density=1.0, views=256, res=RES, max_radius=0.1),
+    "c4": dict(points=100_000_000, boxes=12, density=100.0, views=1024, res=None, max_radius=0.1),
 }
 
 
@@ -116,7 +118,8 @@ def workload_name(args, n_points, n_views):
     else:
         shape = "%d views (%s, fx=0.75W)" % (n_views, "/".join("%dx%d" % r for r in w["res"]))
     dens = "" if w["density"] <= 1.0 else ", per-surface density log-uniform over %gx" % w["density"]
-    return "batched render of %s over a %d-point synthetic room, %d boxes%s" % (shape, n_points, w["boxes"], dens)
+    return "batched render of %s over a %d-point synthetic room, %d boxes%s, max_radius %g" % (
+        shape, n_points, w["boxes"], dens, w["max_radius"])
 
 
 class Clocks:
@@ -175,10 +178,10 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def traffic_per_ray():
-    """DRAM bytes per ray of the batched marcher from the committed ncu
-    summary (profiles/march_batch_traffic.json), or None."""
-    p = os.path.join(ROOT, "profiles", "march_batch_traffic.json")
+def capture_figures(name):
+    """Figures of a committed ncu summary (profiles/<name>.json: DRAM bytes
+    per unit, issue and occupancy counters), or None."""
+    p = os.path.join(ROOT, "profiles", name + ".json")
     if os.path.exists(p):
         return json.load(open(p))
     return None
@@ -197,27 +200,53 @@ def hit_checksum(keep) -> int:
     return total
 
 
-def cpu_sample_render(sc, views, radii_clamped, n_rays, seed, threads=0):
-    """Oracle (the reference marcher loop restated in C, exact 10-NN) on a
-    bounded, seeded sample of rays spread over the views.  Returns
-    (rays, seconds, build_seconds)."""
+def sample_pixels(views, n_rays, seed):
+    """A bounded, seeded sample of pixels spread evenly over the views
+    (sorted linear indices per view)."""
+    rng = np.random.default_rng(seed)
+    per = max(1, n_rays // len(views))
+    return [np.sort(rng.choice(v.pixels, min(per, v.pixels), replace=False)).astype(np.int64) for v in views]
+
+
+def cpu_sample_render(ix, views, panes, radii_clamped, pixels, threads=0):
+    """Oracle (the reference marcher loop restated in C, exact 10-NN per
+    step) over the sampled pixels of each view, each view with the pane
+    distance the device evaluates.  Returns (seconds, [(hit, depth, steps)])."""
+    import oracle
+    jobs = [(oracle.make_view(v.cam2world, v.width, v.height, float(p)), pix)
+            for v, p, pix in zip(views, panes, pixels)]
+    t0 = time.perf_counter()
+    outs = [ix.render(radii_clamped, ov, pix, threads=threads) for ov, pix in jobs]
+    return time.perf_counter() - t0, outs
+
+
+def compare_with_oracle(gpu, cpu):
+    """Counts of disagreements between the GPU frames and the oracle on the
+    sampled pixels: hit index, depth bits, step count where the ray hits,
+    and misses that the GPU marched longer than the oracle (exit culling
+    may only shorten a miss)."""
+    c = {"rays": 0, "hit_mismatch": 0, "depth_bit_mismatch": 0, "step_mismatch_on_hits": 0,
+         "miss_steps_above_oracle": 0}
+    for (gh, gd, gs), (oh, od, os_) in zip(gpu, cpu):
+        c["rays"] += int(oh.size)
+        c["hit_mismatch"] += int((gh != oh).sum())
+        c["depth_bit_mismatch"] += int((gd.view(np.int32) != od.view(np.int32)).sum())
+        h = oh >= 0
+        c["step_mismatch_on_hits"] += int((gs[h] != os_[h]).sum())
+        c["miss_steps_above_oracle"] += int((gs[~h] > os_[~h]).sum())
+    return c
+
+
+def cpu_radii(sc, threads):
+    """The reference's radii precompute on the host cores (the oracle's
+    exact 2-NN, build and query both timed).  Returns (seconds, build
+    seconds)."""
     import oracle
     t0 = time.perf_counter()
     ix = oracle.Index(sc.xyz)
-    t_build = time.perf_counter() - t0
-    from renderer_ray_marching_gb300 import Renderer  # noqa: F401  (pane below)
-    rng = np.random.default_rng(seed)
-    per = max(1, n_rays // len(views))
-    jobs = []
-    for v, pane in views:
-        pix = rng.choice(v.pixels, min(per, v.pixels), replace=False).astype(np.int64)
-        jobs.append((oracle.make_view(v.cam2world, v.width, v.height, float(pane)), pix))
-    t0 = time.perf_counter()
-    rays = 0
-    for ov, pix in jobs:
-        ix.render(radii_clamped, ov, pix, threads=threads)
-        rays += pix.shape[0]
-    return rays, time.perf_counter() - t0, t_build
+    tb = time.perf_counter() - t0
+    ix.radii(0.0, threads=threads)
+    return time.perf_counter() - t0, tb, ix
 
 
 def run_reference(args):
@@ -228,7 +257,7 @@ def run_reference(args):
     from renderer_ray_marching_gb300 import synthetic as syn  # noqa: F401
     sc, views = workload(args, 0)
     ix = oracle.Index(sc.xyz)
-    radii, _ = ix.radii(0.1)
+    radii, _ = ix.radii(workload_spec(args)["max_radius"])
     # the pane of each view as the reference evaluates it (device tanf); on
     # the CPU path the host tanf stands in
     import math
@@ -273,7 +302,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     import torch
-    from renderer_ray_marching_gb300 import Renderer, _abi, synthetic as syn, views_from_specs
+    from renderer_ray_marching_gb300 import Renderer, _abi
 
     ws, rank, local = dist_info()
     dist = ws > 1
@@ -283,6 +312,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda:%d" % local)
     stream = torch.cuda.Stream(device=dev)
+    max_radius = float(workload_spec(args)["max_radius"])
 
     sc, views = workload(args, rank)
     log("workload ready: %d points, %d views" % (sc.xyz.shape[0], len(views)))
@@ -304,7 +334,7 @@ def main():
             r.set_cloud(xyz_d, rgb_d)
             r.build_index()
             em.record(stream)
-            r._check(r._lib.rm_radii_compute(r._h, 0.1, rad_d.data_ptr(), nn_d.data_ptr(), _abi.RM_DEVICE))
+            r._check(r._lib.rm_radii_compute(r._h, max_radius, rad_d.data_ptr(), nn_d.data_ptr(), _abi.RM_DEVICE))
             e1.record(stream)
             e1.synchronize()
             if i >= args.warmup:
@@ -342,7 +372,7 @@ def main():
         clocks.start()
         starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
         ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        kern_ms, steps_total, hits_total = [], 0, 0
+        kern_ms, steps_total, st = [], 0, {}
         for k in range(args.steps):
             starts[k].record(stream)
             r.render_batch_into(views, frames, device=True, cviews=cviews)
@@ -350,7 +380,6 @@ def main():
             st = r.stats()  # synchronises; kernel time from events inside the graph
             kern_ms.append(st["kernel_ms"])
             steps_total = st["steps"]
-            hits_total = st.get("hits", 0)
         torch.cuda.synchronize()
         clk = clocks.stop()
         step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -362,7 +391,36 @@ def main():
         value = ws * total_rays / (t_step * 1e-3) / 1e6
         hits_total = int(sum(int((h >= 0).sum().item()) for _, h in keep))
         hit_sum = hit_checksum(keep)
+        walk = {"leaves_per_warp_step": round(st["packet_leaves"] / max(st["warp_steps"], 1), 2),
+                "nodes_per_warp_step": round(st["packet_nodes"] / max(st["warp_steps"], 1), 2),
+                "lane_steps_per_warp_step": round(st["packet_steps"] / max(st["warp_steps"], 1), 2),
+                "queue_spills": st["queue_spills"], "dfs_walks": st["dfs_walks"],
+                "search_errors": st["search_errors"]}
         checks = {}
+
+        # ---- the same batch again with per-pixel step counts: its hit maps
+        # must equal the timed ones, and a seeded pixel sample of it is
+        # compared with the oracle below
+        sample = None
+        if rank == 0 and not args.no_cpu_baseline:
+            steps_bufs = []
+            for i, v in enumerate(views):
+                sb = torch.empty((v.height, v.width), dtype=torch.int32, device=dev)
+                frames[i].steps = sb.data_ptr()
+                steps_bufs.append(sb)
+            r.render_batch_into(views, frames, device=True, cviews=cviews)
+            r.synchronize()
+            checks["verify_render_equals_timed"] = hit_checksum(keep) == hit_sum
+            pixels = sample_pixels(views, args.cpu_rays, 7)
+            gpu_sample = []
+            for (rgbd, hit), sb, pix in zip(keep, steps_bufs, pixels):
+                ip = torch.from_numpy(pix).to(dev)
+                gpu_sample.append((hit.reshape(-1)[ip].cpu().numpy(), rgbd.reshape(-1, 4)[ip, 3].cpu().numpy(),
+                                   sb.reshape(-1)[ip].cpu().numpy()))
+            for i in range(len(views)):
+                frames[i].steps = None
+            del steps_bufs
+            sample = (pixels, gpu_sample, r.view_pane(views))
 
         # ---- the same batch with one independent tree walk per ray (the
         # reference's execution model) instead of the warp packet walk
@@ -398,6 +456,8 @@ def main():
         # ---- e2e: host buffers through the C ABI (views in, RGBA32F images out)
         e2e, h2d, d2h = None, 0, 0
         if not args.skip_e2e:
+            del keep, frames
+            torch.cuda.empty_cache()
             host_frames = (_abi.RmFrame * len(views))()
             host_keep = []
             for i, v in enumerate(views):
@@ -415,6 +475,7 @@ def main():
             d2h = total_rays * 16
             log("e2e %.1f ms (last call's batched launch %.1f ms on the device)" % (
                 1e3 * float(np.mean(e2e_t)), r.stats()["kernel_ms"]))
+            del host_keep
 
         # ---- forward / forward+backward per 1067x690 view on a 1M-point cloud
         fb = {"fwd_ms": None, "fwdbwd_ms": None, "ratio": None}
@@ -430,13 +491,25 @@ def main():
     kms = float(np.median(kern_ms))
     alg_bytes = 20 * total_rays + 16 * hits_total + 160 * steps_total
     achieved = alg_bytes / (kms * 1e-3) / 1e9
-    tr = traffic_per_ray()
-    traffic = None if tr is None else int(tr["dram_bytes_per_ray"] * total_rays)
+    mc = capture_figures("march_batch_traffic") or {}
+    traffic = int(mc["dram_bytes_per_ray"] * total_rays) if "dram_bytes_per_ray" in mc else None
+    n_pts = int(sc.xyz.shape[0])
+    radii_s = float(np.median(radii_ms)) * 1e-3
+    rc = capture_figures("radii_traffic") or {}
+    radii_roof = {"bound": "hbm", "kernel": "index build + k_radii_packet",
+                  "achieved": round(136 * n_pts / radii_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+                  "frac": round(136 * n_pts / radii_s / 1e9 / peak, 4),
+                  "bytes_model": "136 B/point: 16 B point read, 64 B radix sort, 32 B record gather, "
+                                 "16 B query read, 8 B radius + neighbour write",
+                  "traffic": int(rc["dram_bytes_per_query"] * n_pts) if "dram_bytes_per_query" in rc else None,
+                  "dram_bytes_per_query": rc.get("dram_bytes_per_query"),
+                  "query_issue_active_pct": rc.get("sm_issue_active_pct")}
     out = {"metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(t_step, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": workload_name(args, sc.xyz.shape[0], len(views)),
-                      "points": int(sc.xyz.shape[0]), "views": len(views), "rays_per_step": int(total_rays),
+           "config": {"workload": workload_name(args, n_pts, len(views)),
+                      "points": n_pts, "views": len(views), "rays_per_step": int(total_rays),
+                      "max_radius": max_radius,
                       "l2": "inputs larger than L2 (cloud + index >= 0.8 GB), no flush",
                       "launch": tune, "parallelism": "replicas" if ws > 1 else "single"},
            "plain_mrays_s": None if plain is None else round(plain, 3),
@@ -447,6 +520,7 @@ def main():
            "fwd_ms_per_view": fb["fwd_ms"], "fwdbwd_ms_per_view": fb["fwdbwd_ms"],
            "fwdbwd_over_fwd": fb["ratio"],
            "steps_per_ray": round(steps_total / total_rays, 3), "hit_fraction": round(hits_total / total_rays, 4),
+           "walk": walk,
            "checks": checks,
            "e2e": {"value": None if e2e is None else round(e2e, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(h2d),
                    "d2h_bytes_per_step": int(d2h)},
@@ -454,23 +528,42 @@ def main():
                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                         "bytes_model": "20 B out + 16 B colour per hit + 160 B per distance step (10 float4 candidates)",
-                        "sm_issue_active_pct": None if tr is None else tr.get("sm_issue_active_pct"),
-                        "l2_hit_pct": None if tr is None else tr.get("l2_hit_pct"),
-                        "kernel_ms": round(kms, 3)},
+                        "kernel_ms": round(kms, 3),
+                        "binding_bound": "instruction issue (the index is L2-resident); figures below from the "
+                                         "committed capture " + str(mc.get("source")),
+                        "sm_issue_active_pct": mc.get("sm_issue_active_pct"),
+                        "eligible_warps_per_scheduler": mc.get("eligible_warps_per_scheduler"),
+                        "warp_inst_per_lane_step": mc.get("warp_inst_per_lane_step"),
+                        "warp_inst_per_warp_step": mc.get("warp_inst_per_warp_step"),
+                        "l2_hit_pct": mc.get("l2_hit_pct")},
+           "roofline_radii": radii_roof,
            "clocks": clk,
            "gpu_launches": 2 * args.steps}
-    if rank == 0 and not args.no_cpu_baseline:
-        import math
-        vp = [(v, np.float32(np.float32(v.width) / (np.float32(2.0) * np.float32(math.tan(np.float32(0.5) * np.float32(v.fov))))))
-              for v in views]
-        rad_h = np.minimum(rad_d.cpu().numpy(), np.float32(0.1))
+    if sample is not None:
         cores = os.cpu_count() or 1
-        rays, secs, tb = cpu_sample_render(sc, vp, rad_h, args.cpu_rays, 7, threads=cores)
+        pixels, gpu_sample, panes = sample
+        rad_h = np.minimum(rad_d.cpu().numpy(), np.float32(max_radius))
+        t0 = time.perf_counter()
+        import oracle
+        ix = oracle.Index(sc.xyz)
+        tb = time.perf_counter() - t0
+        secs, cpu_out = cpu_sample_render(ix, views, panes, rad_h, pixels, threads=cores)
+        rays = int(sum(p.size for p in pixels))
         log("cpu baseline %d rays %.1f s (build %.1f s)" % (rays, secs, tb))
+        checks["oracle_sample"] = compare_with_oracle(gpu_sample, cpu_out)
+        log("oracle sample %s" % checks["oracle_sample"])
         out["cpu_baseline"] = {"value": round(rays / secs / 1e6, 5), "unit": "Mrays/s", "cores": cores,
                                "kind": "port",
-                               "sample": "%d rays over %d views, oracle kd-tree (build %.1f s, not timed)" % (
-                                   rays, len(vp), tb)}
+                               "sample": "%d rays (%d per view over %d views), oracle kd-tree (build %.1f s, not "
+                                         "timed); the same pixels are compared with the GPU frames" % (
+                                             rays, pixels[0].size, len(views), tb)}
+        del ix
+        rsecs, rbuild, _ = cpu_radii(sc, cores)
+        log("cpu radii %.1f s (build %.1f s)" % (rsecs, rbuild))
+        out["cpu_baseline_radii"] = {"value": round(n_pts / rsecs / 1e6, 4), "unit": "Mqueries/s", "cores": cores,
+                                     "kind": "port",
+                                     "sample": "all %d points: oracle kd-tree build + exact self-inclusive 2-NN, "
+                                               "both timed (build %.1f s)" % (n_pts, rbuild)}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:
@@ -494,7 +587,7 @@ def fwd_bwd(args, dev, stream, rank, scene=None, views=None):
     for rr, x, c in ((r, sc.xyz, sc.rgb), (rt, xt, ct)):
         rr.set_cloud(x, c)
         rr.build_index()
-        rr.compute_radii(0.1)
+        rr.compute_radii(0.1)  # -r default (main.cu:70)
     n = sc.xyz.shape[0]
     tg = [rt.render(v, outputs=("rgbd", "hit"), device=True) for v in views]
     rt.close()

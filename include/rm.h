@@ -99,6 +99,10 @@ typedef struct {
                             walk does not split; kept for layout, always 0) */
   int64_t search_errors; /* searches that hit a self-check bound (0 unless the index is broken) */
   float kernel_ms;       /* device time of the last render launch (graph for the batch) */
+  int64_t queue_spills;  /* best-first walk: pending nodes moved from the 32-entry register queue
+                            to the warp's shared-memory overflow stack */
+  int64_t dfs_walks;     /* best-first walks whose overflow stack filled too, so that they
+                            finished in depth-first order (exact either way) */
 } rm_stats;
 
 /* Marcher launch parameters (picked by rm_autotune or set by hand). */
@@ -209,10 +213,13 @@ int64_t rm_cloud_size(const rm_ctx* ctx);
  * every GPU loading the library holds until exit.  At most
  * RM_NOALLOC_MAX_VIEWS views per call (more returns RM_ERR_LIMIT); the cloud
  * must be non-empty.  The first call on a device looks up the array's device
- * address; make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race, so serialise them.  Returns after the
- * frames are written (it synchronises the context's stream).  rm_get_stats
- * does not count its work. */
+ * address; make it before any stream capture.  That address is kept for the
+ * process's life: it belongs to the device's primary context (the CUDA
+ * runtime's own), and a cudaDeviceReset after the first call invalidates it.
+ * All calls share the array: calls that overlap on the GPU race, so
+ * serialise them.  Returns after the frames are written (it synchronises the
+ * context's stream).  rm_get_stats does not count its work: after this call
+ * it reports zeros until the next rm_render or rm_render_batch. */
 #define RM_NOALLOC_MAX_VIEWS 1024
 #define RM_NOALLOC_SCRATCH_BYTES (256 + 1024 * 136)
 rm_status rm_render_batch_noalloc(rm_ctx* ctx, const rm_view* views, int32_t n,

@@ -15,6 +15,7 @@ from . import build as _build
 
 RM_OK, RM_ERR_INVALID, RM_ERR_STATE, RM_ERR_CUDA, RM_ERR_OOM, RM_ERR_LIMIT, RM_ERR_KERNEL = range(7)
 RM_HOST, RM_DEVICE = 0, 1
+RM_NOALLOC_MAX_VIEWS = 1024  # include/rm.h
 STATUS_NAMES = {0: "RM_OK", 1: "RM_ERR_INVALID", 2: "RM_ERR_STATE", 3: "RM_ERR_CUDA",
                 4: "RM_ERR_OOM", 5: "RM_ERR_LIMIT", 6: "RM_ERR_KERNEL"}
 
@@ -48,7 +49,8 @@ class RmStats(ctypes.Structure):
                 ("packet_steps", ctypes.c_int64), ("solo_steps", ctypes.c_int64),
                 ("packet_leaves", ctypes.c_int64), ("packet_nodes", ctypes.c_int64),
                 ("warp_steps", ctypes.c_int64), ("split_steps", ctypes.c_int64),
-                ("search_errors", ctypes.c_int64), ("kernel_ms", ctypes.c_float)]
+                ("search_errors", ctypes.c_int64), ("kernel_ms", ctypes.c_float),
+                ("queue_spills", ctypes.c_int64), ("dfs_walks", ctypes.c_int64)]
 
 
 class RmLaunch(ctypes.Structure):

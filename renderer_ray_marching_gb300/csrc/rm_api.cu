@@ -332,9 +332,8 @@ rm_status rm_radii_compute(rm_ctx* ctx, float max_radius, float* radii_out, int3
       dn = nn_out ? reinterpret_cast<int32_t*>(c.staging_out.ptr<float>() + n) : nullptr;
     }
     CK(cudaMemsetAsync(err_counter(c), 0, 8, c.stream));
-    launch_radii(c, max_radius, dr, dn);
+    launch_radii(c, max_radius, dr, dn);  // also sets the records' radii
     CK(cudaGetLastError());
-    launch_set_radius(c);
     refresh_max_radius(c);
     check_kernel_errors(c);
     if (loc == RM_HOST) {
@@ -406,6 +405,7 @@ rm_status rm_render(rm_ctx* ctx, const rm_view* view, const rm_frame* out, int32
     }
     CK(cudaMemsetAsync(counters(c), 0, kCounters * 8, c.stream));
     CK(cudaMemsetAsync(err_counter(c), 0, 8, c.stream));
+    c.stats_from_noalloc = false;
     if (c.n == 0) {
       // empty cloud: every ray misses (no candidate ever comes within MIN_DIST)
       if (f.rgbd) CK(cudaMemsetAsync(f.rgbd, 0, npix * 16, c.stream));
@@ -491,7 +491,7 @@ void enqueue_batch(Ctx& c, int n, int64_t items, const rm_launch& L) {
     CK(cudaMemsetAsync(c.queue.p, 0, 8, c.stream));
     CK(cudaMemsetAsync(counters(c), 0, kCounters * 8, c.stream));
     CK(cudaMemsetAsync(err_counter(c), 0, 8, c.stream));
-    launch_render_batch(c, c.views.ptr<ViewDev>(), n, items, L, counters(c));
+    launch_render_batch(c, c.views.ptr<ViewDev>(), n, items, L, c.queue.ptr<unsigned long long>(), counters(c));
     cudaError_t e = cudaStreamEndCapture(c.stream, &g);
     if (e != cudaSuccess) throw CudaError(std::string("graph capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&c.graph_exec, g, 0);
@@ -577,6 +577,7 @@ rm_status rm_render_batch(rm_ctx* ctx, const rm_view* views, int32_t n, const rm
     }
     c.views.reserve((size_t)n * sizeof(ViewDev));
     enqueue_batch(c, n, items, c.launch);
+    c.stats_from_noalloc = false;
     if (loc == RM_HOST) {
       for (int v = 0; !direct && v < n; ++v) {
         size_t np = (size_t)views[v].width * views[v].height;
@@ -612,6 +613,10 @@ rm_status rm_get_launch(rm_ctx* ctx, rm_launch* launch) {
 rm_status rm_get_stats(rm_ctx* ctx, rm_stats* stats) {
   return guarded(ctx, [&](Ctx& c) -> rm_status {
     if (!stats) return fail(c, RM_ERR_INVALID, "rm_get_stats: null");
+    if (c.stats_from_noalloc) {
+      *stats = rm_stats{};
+      return RM_OK;
+    }
     unsigned long long h[kCounters];
     CK(cudaMemcpyAsync(h, counters(c), sizeof(h), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
@@ -630,6 +635,8 @@ rm_status rm_get_stats(rm_ctx* ctx, rm_stats* stats) {
     c.stats.warp_steps = (int64_t)h[8];
     c.stats.split_steps = (int64_t)h[9];
     c.stats.search_errors = (int64_t)h[3];
+    c.stats.queue_spills = (int64_t)h[10];
+    c.stats.dfs_walks = (int64_t)h[11];
     c.stats.kernel_ms = ms;
     *stats = c.stats;
     return RM_OK;

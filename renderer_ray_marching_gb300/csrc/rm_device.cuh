@@ -424,10 +424,14 @@ struct PacketStack {
 };
 
 // Shared memory of the best-first walk: the depth-first stack and staged
-// leaf of PacketStack plus the queue's overflow stack.
+// leaf of PacketStack plus the queue's overflow stack, and two event counts
+// kept by lane 0 (entries moved to the overflow stack; walks that fell back
+// to depth-first order) for the launch statistics.
 constexpr int PKT_OVERFLOW = 256;
 struct PacketQueue : PacketStack {
   uint32_t over[PKT_OVERFLOW];
+  unsigned n_spill;
+  unsigned n_dfs;
 };
 
 __device__ __forceinline__ void list_consider_unique(KSet& L, float d, int32_t s, float r,
@@ -637,9 +641,13 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
   // the bounds are still loose.
   auto spill = [&](uint32_t code) {
     if (!dfs && osp < PKT_OVERFLOW) {
-      if (lane == 0) ps.over[osp] = code;
+      if (lane == 0) {
+        ps.over[osp] = code;
+        ++ps.n_spill;
+      }
       ++osp;
     } else {
+      if (!dfs && lane == 0) ++ps.n_dfs;
       dfs = true;
       if (sp + fsp < PSTACK && lane == 0) ps.code[PSTACK - 1 - fsp] = code;
       ++fsp;

@@ -105,6 +105,10 @@ struct Ctx {
 
   rm_launch launch{8, 4, 1, 5, 1};
   rm_stats stats{};
+  // set by the allocation-free batch, whose counters live in its static
+  // scratch: rm_get_stats then reports zeros instead of the counters and
+  // time of an earlier render
+  bool stats_from_noalloc = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
   // cached CUDA graph of the batched launch
@@ -150,12 +154,9 @@ void launch_knn(Ctx& c, const float* q, int stride, int64_t m, int k, int32_t* i
 void launch_view_pane(Ctx& c, const rm_view* views_dev, int n, float* pane_out);
 void launch_render_plain(Ctx& c, const rm_view& v, float4* rgbd, int32_t* hit, float* depth,
                          int32_t* steps, unsigned long long* counters);
-void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_tiles,
-                         const rm_launch& L, unsigned long long* counters);
+void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
+                         const rm_launch& L, unsigned long long* queue, unsigned long long* counters);
 void launch_prepare_views(Ctx& c, ViewDev* views_dev, int n, unsigned long long* counters);
-void launch_render_batch_queue(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
-                               const rm_launch& L, unsigned long long* queue,
-                               unsigned long long* counters);
 
 // rm_backward.cu
 void launch_backward(Ctx& c, const ViewDev* views_dev, int n, int64_t total_pixels,

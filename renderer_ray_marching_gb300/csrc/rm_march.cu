@@ -96,8 +96,10 @@ struct ViewArgs {
 // counters: [0] steps, [1] rays, [2] hits, [3] search errors,
 //           [4] packet lane-steps, [5] per-lane lane-steps, [6] leaves scanned by packets,
 //           [7] nodes expanded by packets, [8] warp steps, [9] warp steps split in two packets
-//           (no longer split: always 0)
-enum { C_STEPS, C_RAYS, C_HITS, C_BAD, C_COOP, C_SOLO, C_LEAVES, C_NODES, C_WSTEPS, C_SPLIT, C_N };
+//           (no longer split: always 0), [10] queue entries moved to the overflow stack,
+//           [11] packet walks that fell back to depth-first order
+enum { C_STEPS, C_RAYS, C_HITS, C_BAD, C_COOP, C_SOLO, C_LEAVES, C_NODES, C_WSTEPS, C_SPLIT, C_SPILL, C_DFS,
+       C_N };
 
 // Per-warp shared state.  The view of the current item and the statistics
 // live here rather than in registers: they are read or bumped at a ray's
@@ -221,6 +223,10 @@ __device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int t
 __device__ __forceinline__ void clear_counters(WarpSmem& sm) {
   const int lane = threadIdx.x & 31;
   if (lane < C_N) sm.cnt[lane] = 0ull;
+  if (lane == 0) {
+    sm.ps.n_spill = 0;
+    sm.ps.n_dfs = 0;
+  }
   __syncwarp();
 }
 
@@ -234,6 +240,8 @@ __device__ __forceinline__ void flush_counters(WarpSmem& sm, unsigned long long*
   if (lane < C_N) {
     unsigned long long v = lane == C_COOP ? (SEARCH == 1 ? sm.cnt[C_STEPS] : 0ull)
                          : lane == C_SOLO ? (SEARCH == 0 ? sm.cnt[C_STEPS] : 0ull)
+                         : lane == C_SPILL ? (unsigned long long)sm.ps.n_spill
+                         : lane == C_DFS ? (unsigned long long)sm.ps.n_dfs
                          : sm.cnt[lane];
     if (v) atomicAdd(counters + lane, v);
   }
@@ -406,37 +414,11 @@ void launch_prepare_views(Ctx& c, ViewDev* views_dev, int n, unsigned long long*
   k_prepare_views<<<(n + 127) / 128, 128, 0, c.stream>>>(views_dev, n);
 }
 
+// `queue` is the work-queue counter the launch's warps pull items from (zero
+// before the launch): the context's own for rm_render_batch, the static
+// scratch's for the allocation-free entry point.
 void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_items, const rm_launch& L,
-                         unsigned long long* counters) {
-  BatchArgs a;
-  a.views = views_dev;
-  a.nviews = n;
-  a.total_items = total_items;
-  a.tile_w = L.tile_w;
-  a.tile_h = L.tile_h;
-  a.rpl = L.rays_per_lane;
-  unsigned long long* queue = c.queue.ptr<unsigned long long>();
-  int grid = c.sm_count * (L.ctas_per_sm > 0 ? L.ctas_per_sm : 4);
-  MarchParams mp = march_params(c);
-  auto go = [&](auto kern) {
-    kern<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, mp, queue, counters);
-  };
-  const int cps = L.ctas_per_sm;
-  if (mp.search == 1) {
-    if (cps >= 8) go(k_march_batch<1, 8>);
-    else if (cps >= 6) go(k_march_batch<1, 6>);
-    else if (cps >= 5) go(k_march_batch<1, 5>);
-    else go(k_march_batch<1, 4>);
-  } else {
-    go(k_march_batch<0, 4>);
-  }
-}
-
-// Same launch as launch_render_batch with a caller-supplied queue counter
-// (used by the allocation-free entry point, whose scratch is static).
-void launch_render_batch_queue(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
-                               const rm_launch& L, unsigned long long* queue,
-                               unsigned long long* counters) {
+                         unsigned long long* queue, unsigned long long* counters) {
   BatchArgs a;
   a.views = views_dev;
   a.nviews = n;

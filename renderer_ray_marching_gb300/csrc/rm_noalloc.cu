@@ -21,7 +21,10 @@
 // In host code the array's name is only a host-side stand-in for the symbol,
 // not a device address.  The device address comes from cudaGetSymbolAddress,
 // taken once per device, with that device current, by the first call made
-// on it; make that first call before any stream capture begins.
+// on it; make that first call before any stream capture begins.  The address
+// is kept for the life of the process, so it belongs to the device's primary
+// context (the one the CUDA runtime uses): after a cudaDeviceReset it is no
+// longer valid (neither is any rm_ctx created before the reset).
 #include "rm_internal.h"
 
 #include <cmath>
@@ -91,6 +94,7 @@ extern "C" rm_status rm_render_batch_noalloc(rm_ctx* ctx, const rm_view* views, 
   ViewDev* views_dev = reinterpret_cast<ViewDev*>(base + kHeaderBytes);
 
   const rm_launch L = c.launch;
+  c.stats_from_noalloc = true;  // its counters stay in the static scratch
   int64_t items = 0;
   for (int v = 0; v < n; ++v) {
     ViewDev& d = g_host_views[v];
@@ -114,13 +118,12 @@ extern "C" rm_status rm_render_batch_noalloc(rm_ctx* ctx, const rm_view* views, 
   if (e == cudaSuccess) e = cudaMemsetAsync(base, 0, kHeaderBytes, c.stream);
   if (e != cudaSuccess) return fail(c, RM_ERR_CUDA, cudaGetErrorString(e));
   launch_prepare_views(c, views_dev, n, counters);
-  launch_render_batch_queue(c, views_dev, n, items, L, queue, counters);
+  launch_render_batch(c, views_dev, n, items, L, queue, counters);
   e = cudaGetLastError();
   unsigned long long bad = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, counters + 3, sizeof(bad), cudaMemcpyDeviceToHost, c.stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
   if (e != cudaSuccess) return fail(c, RM_ERR_CUDA, cudaGetErrorString(e));
   if (bad) return fail(c, RM_ERR_KERNEL, "a nearest-neighbour search did not complete");
-  c.stats.kernel_ms = -1.0f;
   return RM_OK;
 }

@@ -4,10 +4,10 @@
 // nearestKernel with k = 2 (kdtree_cuda_3d_index.cu:132-154, one thread per
 // query, result arrays in global memory), followed by a host loop doing 2N
 // synchronous device_reference copies for sqrt, and a separate clamp pass
-// (main.cu:144-149).  Here one kernel does search, sqrt, clamp and the
-// scatter back to cloud order.  Threads walk the points in index (Morton)
-// order, so the 32 queries of a warp are spatial neighbours and their tree
-// walks touch the same groups and leaves (L1/L2 hits).
+// (main.cu:144-149).  Here one kernel does the search and the sqrt for every
+// point, in index (Morton) order, so the 32 queries of a warp are spatial
+// neighbours and their tree walks touch the same groups and leaves (L1/L2
+// hits); short passes then write the results in cloud order and clamp.
 #include "rm_internal.h"
 
 namespace rm {
@@ -34,15 +34,26 @@ k_radii(IndexDev ix, float max_radius, float* __restrict__ radii_out, int32_t* _
 // neighbours along the Morton curve), seeds each lane's 2-NN list with the
 // point itself and its next (or previous) record, and walks the tree once
 // for all 32 (packet_knn).  Same results as k_radii.
+//
+// Memory traffic.  Warps take their 32-point chunks from a global counter
+// in sorted order, so every resident warp works inside one window of about
+// (resident warps x 32) consecutive records -- a few MB, which stays in L2
+// while neighbouring warps re-read the same leaves.  (A grid-stride loop
+// spreads the resident warps over strides of the whole array, and their
+// leaf reads miss L2.)  Results go out in sorted order with coalesced
+// stores; k_radii_to_cloud moves them to cloud order afterwards.
 constexpr int RADII_WARPS = 4;
 __global__ void __launch_bounds__(32 * RADII_WARPS)
-k_radii_packet(IndexDev ix, float max_radius, float* __restrict__ radii_out, int32_t* __restrict__ nn_out,
-               float* __restrict__ radii_clamped, unsigned long long* __restrict__ err) {
+k_radii_packet(IndexDev ix, float* __restrict__ r_sorted, int32_t* __restrict__ nn_sorted,
+               unsigned long long* __restrict__ next, unsigned long long* __restrict__ err) {
   __shared__ PacketStack stacks[RADII_WARPS];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t nwarps = (int64_t)gridDim.x * RADII_WARPS;
   unsigned leaves = 0, nodes = 0;
-  for (int64_t wbase = ((int64_t)blockIdx.x * RADII_WARPS + warp) * 32; wbase < ix.n; wbase += nwarps * 32) {
+  while (true) {
+    unsigned long long chunk = 0;
+    if (lane == 0) chunk = atomicAdd(next, 1ull);
+    const int64_t wbase = (int64_t)__shfl_sync(0xffffffffu, chunk, 0) * 32;
+    if (wbase >= ix.n) break;
     const int64_t s = wbase + lane;
     const bool active = s < ix.n;
     float4 q = active ? __ldg(ix.rec + s) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -58,11 +69,38 @@ k_radii_packet(IndexDev ix, float max_radius, float* __restrict__ radii_out, int
     }
     if (!packet_knn(ix, active, q.x, q.y, q.z, L, stacks[warp], leaves, nodes) && active) atomicAdd(err, 1ull);
     if (active) {
-      float r = __fsqrt_rn(L.d[1]);
-      int32_t i = __ldg(ix.perm + s);
-      if (radii_out) radii_out[i] = r;
-      if (nn_out) nn_out[i] = L.s[1] >= 0 ? __ldg(ix.perm + L.s[1]) : -1;
-      radii_clamped[i] = (max_radius > 0.0f && r > max_radius) ? max_radius : r;
+      // sqrt of the second entry (main.cu:111); +inf when the cloud has one point
+      r_sorted[s] = __fsqrt_rn(L.d[1]);
+      nn_sorted[s] = L.s[1] >= 0 ? __ldg(ix.perm + L.s[1]) : -1;
+    }
+  }
+}
+
+// Sorted-order radii to cloud order (main.cu:110-113 leaves them in PLY
+// order), one output array per launch.  Each launch reads its sorted input
+// and perm once, streaming (evict-first), and scatters 4-byte values over
+// one array of 4 N bytes; at up to about 25M points that array fits in L2,
+// where the scattered stores merge into whole sectors before they reach
+// DRAM.  MODE 0: unclamped radius; 1: neighbour's cloud index; 2: radius
+// clamped to max_radius (main.cu:144-149) -- the context's render radii --
+// also written into the records' .w in sorted order.
+template <int MODE>
+__global__ void k_radii_to_cloud(const float* __restrict__ r_sorted, const int32_t* __restrict__ nn_sorted,
+                                 const int32_t* __restrict__ perm, int64_t n, float max_radius,
+                                 void* __restrict__ out, float4* __restrict__ rec) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i = __ldcs(perm + s);
+    if (MODE == 1) {
+      static_cast<int32_t*>(out)[i] = __ldcs(nn_sorted + s);
+    } else {
+      float r = __ldcs(r_sorted + s);
+      if (MODE == 2) {
+        r = (max_radius > 0.0f && r > max_radius) ? max_radius : r;
+        float4 c = rec[s];  // whole records rewritten: full-sector stores
+        c.w = r;
+        rec[s] = c;
+      }
+      static_cast<float*>(out)[i] = r;
     }
   }
 }
@@ -93,14 +131,36 @@ static int blocks_for(const Ctx& c, int64_t n, int threads) {
   return (int)b;
 }
 
+// Radii of every point: search, then cloud-order outputs, the context's
+// clamped radii and the records' radius lanes.
 void launch_radii(Ctx& c, float max_radius, float* radii_out, int32_t* nn_out) {
   unsigned long long* err = c.scalars.ptr<unsigned long long>() + 8;
   if (c.launch.search == 1) {
-    k_radii_packet<<<blocks_for(c, c.n, 32 * RADII_WARPS), 32 * RADII_WARPS, 0, c.stream>>>(
-        c.index(), max_radius, radii_out, nn_out, c.radii_clamped.ptr<float>(), err);
+    // sorted-order results in the radix sort's key buffers (N x 4 B each,
+    // free once the index is built)
+    float* r_sorted = c.keys[0].ptr<float>();
+    int32_t* nn_sorted = c.keys[1].ptr<int32_t>();
+    unsigned long long* next = c.queue.ptr<unsigned long long>() + 1;
+    CK(cudaMemsetAsync(next, 0, sizeof(unsigned long long), c.stream));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_radii_packet, 32 * RADII_WARPS, 0));
+    const int64_t chunks = (c.n + 31) / 32;
+    int64_t grid = (int64_t)c.sm_count * (per_sm > 0 ? per_sm : 1);
+    const int64_t need = (chunks + RADII_WARPS - 1) / RADII_WARPS;
+    if (grid > need) grid = need;
+    k_radii_packet<<<(unsigned)grid, 32 * RADII_WARPS, 0, c.stream>>>(c.index(), r_sorted, nn_sorted, next, err);
+    const int g = blocks_for(c, c.n, 256);
+    const int32_t* perm = c.perm.ptr<int32_t>();
+    if (radii_out)
+      k_radii_to_cloud<0><<<g, 256, 0, c.stream>>>(r_sorted, nn_sorted, perm, c.n, max_radius, radii_out, nullptr);
+    if (nn_out)
+      k_radii_to_cloud<1><<<g, 256, 0, c.stream>>>(r_sorted, nn_sorted, perm, c.n, max_radius, nn_out, nullptr);
+    k_radii_to_cloud<2><<<g, 256, 0, c.stream>>>(r_sorted, nn_sorted, perm, c.n, max_radius,
+                                                 c.radii_clamped.ptr<float>(), c.rec.ptr<float4>());
   } else {
     k_radii<<<blocks_for(c, c.n, 128), 128, 0, c.stream>>>(c.index(), max_radius, radii_out, nn_out,
                                                            c.radii_clamped.ptr<float>(), err);
+    launch_set_radius(c);
   }
 }
 

@@ -322,24 +322,34 @@ int run(const Args& a) {
     const size_t nv = pending.size();
     unsigned nt = std::thread::hardware_concurrency();
     nt = (unsigned)std::max<size_t>(1, std::min<size_t>({nt ? nt : 4u, 32u, nv}));
-    std::vector<std::exception_ptr> err(nt);
+    // A view whose files could not be written keeps its .lock file, as a
+    // run of the reference that stops in that view's output would; every
+    // view written before or after it is still reported and unlocked, and
+    // the first error is raised after that.
+    std::vector<std::exception_ptr> err(nv);
     std::vector<std::thread> workers;
     for (unsigned w = 0; w < nt; ++w)
       workers.emplace_back([&, w] {
-        try {
-          for (size_t i = w; i < nv; i += nt) save_outputs(pending[i], images[i]);
-        } catch (...) {
-          err[w] = std::current_exception();
+        for (size_t i = w; i < nv; i += nt) {
+          try {
+            save_outputs(pending[i], images[i]);
+          } catch (...) {
+            err[i] = std::current_exception();
+          }
         }
       });
     for (auto& t : workers) t.join();
-    for (auto& e : err)
-      if (e) std::rethrow_exception(e);
+    std::exception_ptr first;
     for (size_t i = 0; i < nv; ++i) {
+      if (err[i]) {
+        if (!first) first = err[i];
+        continue;
+      }
       cout << fs::canonical(fs::absolute(pending[i].out)) << ": " << (float)per << " s" << endl;
       pending[i].lock->unlock();
       fs::remove(pending[i].lock_path);
     }
+    if (first) std::rethrow_exception(first);
   }
   return EXIT_SUCCESS;
 }

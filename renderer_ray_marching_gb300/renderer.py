@@ -275,7 +275,8 @@ class Renderer:
         return {"rays": s.rays, "steps": s.steps, "hits": s.hits, "packet_steps": s.packet_steps,
                 "search_errors": s.search_errors,
                 "solo_steps": s.solo_steps, "packet_leaves": s.packet_leaves, "packet_nodes": s.packet_nodes,
-                "warp_steps": s.warp_steps, "split_steps": s.split_steps, "kernel_ms": s.kernel_ms}
+                "warp_steps": s.warp_steps, "split_steps": s.split_steps, "kernel_ms": s.kernel_ms,
+                "queue_spills": s.queue_spills, "dfs_walks": s.dfs_walks}
 
     # -- backward -------------------------------------------------------------
     def backward(self, views, dl_drgb, dl_ddepth, hit, g_rgb, g_xyz, g_radius):

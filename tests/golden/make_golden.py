@@ -2,7 +2,7 @@
 FLANN CPU kd-tree (oracle/_ref/ref_driver, built by oracle/Makefile.ref from
 the reference tree).  Run where the reference is present:
 
-    make -f oracle/Makefile.ref REF=/root/reference
+    make -f oracle/Makefile.ref REF=<reference checkout>
     python tests/golden/make_golden.py
 
 Fixtures (numpy .npz, seeded synthetic inputs):

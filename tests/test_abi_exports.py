@@ -40,3 +40,13 @@ def test_null_context_is_rejected_not_crashing():
     assert lib.rm_synchronize(None) == _abi.RM_ERR_INVALID
     assert lib.rm_last_error(None) == b"null context"
     assert lib.rm_cloud_size(None) == -1
+
+
+def test_python_constants_and_structs_mirror_the_header():
+    text = open(os.path.join(ROOT, "include", "rm.h")).read()
+    assert int(re.search(r"#define RM_NOALLOC_MAX_VIEWS (\d+)", text).group(1)) == _abi.RM_NOALLOC_MAX_VIEWS
+    end = text.index("} rm_stats;")
+    body = text[text.rindex("typedef struct {", 0, end):end]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"\b(?:int64_t|float)\s+([a-z_]+)\s*;", body)
+    assert fields == [f for f, _ in _abi.RmStats._fields_]

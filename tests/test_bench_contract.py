@@ -54,12 +54,37 @@ class _Args:
 def test_workload_presets():
     c2 = bench.workload_spec(_Args("c2"))
     assert (c2["points"], c2["boxes"], c2["density"], c2["views"]) == (20_000_000, 40, 1.0, 256)
+    assert c2["max_radius"] == 0.1
+    c1 = bench.workload_spec(_Args("c1"))
+    assert (c1["points"], c1["boxes"], c1["views"], c1["res"], c1["max_radius"]) == (2_000_000, 12, 64, None, 0.05)
     assert c2["res"] == [(640, 480), (1068, 690), (1920, 1080)]
     c4 = bench.workload_spec(_Args("c4"))
     assert (c4["points"], c4["boxes"], c4["density"], c4["views"], c4["res"]) == (100_000_000, 12, 100.0, 1024, None)
     assert "per-surface density log-uniform over 100x" in bench.workload_name(_Args("c4"), 100_000_000, 1024)
     small = bench.workload_spec(_Args("c2", points=1000, views=3, resolution="64x48"))
     assert (small["points"], small["views"], small["res"]) == (1000, 3, [(64, 48)])
+
+
+def test_oracle_comparison_counts_every_kind_of_disagreement():
+    import numpy as np
+    oh = np.array([5, -1, 7, 9], np.int32)
+    od = np.array([1.5, 0.0, 2.0, 3.0], np.float32)
+    os_ = np.array([10, 128, 12, 4], np.int32)
+    same = bench.compare_with_oracle([(oh, od, os_)], [(oh, od, os_)])
+    assert same == {"rays": 4, "hit_mismatch": 0, "depth_bit_mismatch": 0, "step_mismatch_on_hits": 0,
+                    "miss_steps_above_oracle": 0}
+    gd = od.copy()
+    gd[2] = np.nextafter(gd[2], np.float32(3))
+    gs = os_.copy()
+    gs[0] += 1
+    gs[1] = 20  # a culled miss stops earlier: not counted
+    gh = oh.copy()
+    gh[3] = 8
+    c = bench.compare_with_oracle([(gh, gd, gs)], [(oh, od, os_)])
+    assert (c["hit_mismatch"], c["depth_bit_mismatch"], c["step_mismatch_on_hits"], c["miss_steps_above_oracle"]) == (
+        1, 1, 1, 0)
+    gs[1] = 129
+    assert bench.compare_with_oracle([(oh, od, gs)], [(oh, od, os_)])["miss_steps_above_oracle"] == 1
 
 
 @pytest.mark.parametrize("flag", ["--workload", "--impl"])

@@ -60,15 +60,16 @@ def loss_grads(pred, tgt):
     return g_rgb, g_d, both
 
 
-def test_fd_fp64_non_silhouette(setup):
-    sc, r, rc, views, pred, tgt, panes = setup
-    v, p, t = views[0], pred[0], tgt[0]
+def fd_check(sc, r, rc, v, pane, p, t, count, seed):
+    """Backward of one view against FP64 central differences on `count`
+    non-silhouette pixels with distinct hit points (Richardson over h, h/2
+    for positions and radii); returns the worst relative error."""
     hit = p["hit"].reshape(-1).astype(np.int32)
     g_rgb_all, _, both = loss_grads(p, t)
-    ov = oracle.make_view(v.cam2world, v.width, v.height, float(panes[0]))
+    ov = oracle.make_view(v.cam2world, v.width, v.height, float(pane))
     col = sc.rgb.astype(np.float32) / np.float32(255.0)
     trgbd = t["rgbd"].reshape(-1, 4).astype(np.float64)
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(seed)
     chosen, seen = [], set()
     for pix in rng.permutation(np.nonzero(both)[0]):
         h = int(hit[pix])
@@ -85,9 +86,9 @@ def test_fd_fp64_non_silhouette(setup):
             continue
         seen.add(h)
         chosen.append((int(pix), h, o.astype(np.float64), d.astype(np.float64)))
-        if len(chosen) == 2000:
+        if len(chosen) == count:
             break
-    assert len(chosen) >= 1000
+    assert len(chosen) >= count // 2
     dl_rgb = np.zeros((v.pixels, 3), np.float32)
     dl_d = np.zeros(v.pixels, np.float32)
     for pix, h, o, d in chosen:
@@ -124,7 +125,45 @@ def test_fd_fp64_non_silhouette(setup):
         err_geo = np.max(np.abs(got[3:] - fd[3:])) / scale
         err_col = np.max(np.abs(got[:3] - fd[:3])) / max(np.max(np.abs(fd[:3])), 1e-3)
         worst = max(worst, err_geo, err_col)
+    return worst, len(chosen)
+
+
+def test_fd_fp64_non_silhouette(setup):
+    sc, r, rc, views, pred, tgt, panes = setup
+    worst, _ = fd_check(sc, r, rc, views[0], panes[0], pred[0], tgt[0], 2000, seed=0)
     assert worst <= TOL, worst
+
+
+def test_fd_fp64_at_the_differentiation_workload_shape():
+    """The differentiation workload's shape: a 1M-point cloud, 16 views at
+    1067x690 (README intrinsics) of which 2 are checked, 1,000 non-silhouette
+    pixels each (2,000 in all) against FP64 central differences."""
+    sc = syn.make_scene(1_000_000, n_boxes=12, seed=4000)
+    views = views_from_specs(syn.make_views(16, seed=4100, boxes=sc.boxes))
+    assert all((v.width, v.height) == (1067, 690) for v in views)
+    rng = np.random.default_rng(5)
+    xyz_t = (sc.xyz + rng.normal(0, 0.005, sc.xyz.shape)).astype(np.float32)
+    rgb_t = np.clip(sc.rgb.astype(np.int32) + rng.integers(-30, 31, sc.rgb.shape), 0, 255).astype(np.uint8)
+    r = Renderer()
+    r.set_cloud(sc.xyz, sc.rgb)
+    r.build_index()
+    radii, _ = r.compute_radii(0.1)
+    rc = np.minimum(radii, np.float32(0.1))
+    rt = Renderer()
+    rt.set_cloud(xyz_t, rgb_t)
+    rt.build_index()
+    rt.compute_radii(0.1)
+    panes = r.view_pane(views)
+    total = 0
+    for i in (0, 1):
+        p = r.render(views[i], outputs=("rgbd", "hit"))
+        t = rt.render(views[i], outputs=("rgbd", "hit"))
+        worst, k = fd_check(sc, r, rc, views[i], panes[i], p, t, 1000, seed=10 + i)
+        assert worst <= TOL, (i, worst)
+        total += k
+    assert total >= 2000
+    r.close()
+    rt.close()
 
 
 def test_autograd_reimplementation(setup):

@@ -113,3 +113,21 @@ def test_cli_radii_count_mismatch_fails_cleanly(workdir):
     fileio.write_radii(bad + ".kdtree.radii", np.ones(99, np.float32))
     rc, so, se = run(["-f", bad, "-m", mj, "-o", str(d / "o3"), "-d"])
     assert rc != 0 and "does not contain the same number of points" in se
+
+
+def test_cli_batch_write_error_keeps_other_views(workdir):
+    """--batch: a view whose files cannot be written makes the run fail, but
+    every other view is still reported and unlocked (only the failed view
+    keeps its .lock file, as a run of the reference stopping there would)."""
+    d, sc, ply, mj, specs = workdir
+    out = str(d / "out_err")
+    os.makedirs(os.path.join(out, "renders", "b_depth.png.npy"))  # the .npy path is a directory
+    rc, so, se = run(["-f", ply, "-m", mj, "-o", out, "-d", "--batch"])
+    assert rc != 0
+    for name in ("a", "c"):
+        p = os.path.realpath(os.path.join(out, "renders", name + "_color.png"))
+        assert any(l.startswith('"%s": ' % p) and l.endswith(" s") for l in so.splitlines()), so
+        assert os.path.exists(os.path.join(out, "renders", name + "_depth.png"))
+        assert not os.path.exists(os.path.join(out, "renders", "." + name + "_color.png.lock"))
+    assert os.path.exists(os.path.join(out, "renders", ".b_color.png.lock"))
+

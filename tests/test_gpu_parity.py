@@ -290,3 +290,37 @@ def test_render_with_duplicate_points_matches_oracle(search):
         assert (oh >= 0).mean() > 0.5
     assert r.stats()["search_errors"] == 0
     r.close()
+
+
+@pytest.mark.parametrize("offset", [1e4, -3.7e3])
+def test_exit_culling_on_a_cloud_far_from_the_origin(offset):
+    """The exit clip (every ray stops where it leaves the box of all centres
+    grown by max radius + MIN_DIST + slack) must not change any result when
+    float spacing is coarse: the room and the cameras moved 10^4 m (spacing
+    about 1 mm, the size of MIN_DIST) or -3.7 km from the origin.  Every
+    pixel of the view is compared with the oracle, which has no clip."""
+    import dataclasses
+    sc = syn.make_scene(100_000, n_boxes=12, seed=21)
+    xyz = (sc.xyz.astype(np.float64) + offset).astype(np.float32)
+    specs = syn.make_views(3, seed=22, boxes=sc.boxes, resolutions=[(200, 150)])
+    moved = []
+    for s in specs:
+        pose = np.array(s.camera_pose, np.float64)
+        pose[:3, 3] += offset
+        moved.append(dataclasses.replace(s, camera_pose=pose))
+    views = views_from_specs(moved)
+    r, radii, _ = make_renderer(xyz, sc.rgb)
+    ix = oracle.Index(xyz)
+    orad, _ = ix.radii(0.0)
+    assert np.array_equal(radii.view(np.int32), orad.view(np.int32))
+    rc = np.minimum(radii, np.float32(0.1))
+    for v, b in zip(views, r.render_batch(views, outputs=("hit", "depth", "steps"), device=False)):
+        oh, od, os_ = ix.render(rc, oracle_view(r, v))
+        gh, gd, gs = b["hit"].reshape(-1), b["depth"].reshape(-1), b["steps"].reshape(-1)
+        assert np.array_equal(gh, oh)
+        assert np.array_equal(gd.view(np.int32), od.view(np.int32))
+        assert np.array_equal(gs[oh >= 0], os_[oh >= 0])
+        assert np.all(gs[oh < 0] <= os_[oh < 0])
+        assert (oh >= 0).mean() > 0.5
+    assert r.stats()["search_errors"] == 0
+    r.close()

@@ -64,6 +64,48 @@ def test_noalloc_matches_batched_render_on_consecutive_calls():
             assert np.array_equal(ref["rgbd"].view(np.int32), got["rgbd"].view(np.int32))
             assert np.array_equal(ref["depth"].view(np.int32), got["depth"].view(np.int32))
             assert (got["hit"] >= 0).any()
+        # its counters stay in the static scratch: the context's statistics
+        # report zeros, not the previous rm_render_batch's figures
+        st = r.stats()
+        assert st["rays"] == 0 and st["steps"] == 0 and st["kernel_ms"] == 0.0
+    r.close()
+
+
+def test_noalloc_allocates_no_device_memory():
+    """The device's free memory is the same before and after a call (after a
+    first call on another view set, which loads the kernels), and a batch of
+    exactly RM_NOALLOC_MAX_VIEWS views, which fills the static view table,
+    still equals rm_render_batch."""
+    torch = pytest.importorskip("torch")
+    sc = syn.make_scene(30_000, n_boxes=6, seed=8)
+    r = Renderer(leaf_size=16)
+    r.set_cloud(sc.xyz, sc.rgb)
+    r.build_index()
+    r.compute_radii(0.1)
+    lib, h = r._lib, r._h
+    small = views_from_specs(syn.make_views(4, seed=30, boxes=sc.boxes, resolutions=[(40, 24)]))
+    full = views_from_specs(syn.make_views(_abi.RM_NOALLOC_MAX_VIEWS, seed=31, boxes=sc.boxes,
+                                           resolutions=[(16, 8), (8, 12), (24, 4)]))
+    c_small = (_abi.RmView * len(small))(*[v.to_c() for v in small])
+    c_full = (_abi.RmView * len(full))(*[v.to_c() for v in full])
+    f_small, b_small = device_frames(torch, small, -7)
+    f_full, b_full = device_frames(torch, full, -7)
+    ref_frames, ref_bufs = device_frames(torch, full, -5)
+    torch.cuda.synchronize()
+    _abi.check(lib, h, lib.rm_render_batch_noalloc(h, c_small, len(small), f_small))
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    _abi.check(lib, h, lib.rm_render_batch_noalloc(h, c_full, len(full), f_full))
+    torch.cuda.synchronize()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert free_after == free_before
+    _abi.check(lib, h, lib.rm_render_batch(h, c_full, len(full), ref_frames, _abi.RM_DEVICE))
+    r.synchronize()
+    for ref, got in zip(host(ref_bufs), host(b_full)):
+        assert np.array_equal(ref["hit"], got["hit"])
+        assert np.array_equal(ref["steps"], got["steps"])
+        assert np.array_equal(ref["rgbd"].view(np.int32), got["rgbd"].view(np.int32))
+        assert np.array_equal(ref["depth"].view(np.int32), got["depth"].view(np.int32))
     r.close()
 
 
