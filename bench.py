@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--cpu-rays", type=int, default=2_000_000,
                     help="rays per CPU-baseline sample (about 12 s of 16-core CPU work at 20M points)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-views", type=int, default=16,
+                    help="views the restated reference GPU path (baseline/ref_gpu) is timed on (0: skip)")
     # switches for short profiling runs (never used for a reported number)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
@@ -235,6 +237,43 @@ def compare_with_oracle(gpu, cpu):
         c["step_mismatch_on_hits"] += int((gs[h] != os_[h]).sum())
         c["miss_steps_above_oracle"] += int((gs[~h] > os_[~h]).sum())
     return c
+
+
+def time_ref_gpu(sc, views, keep, max_radius, dev):
+    """The reference's GPU path, restated (baseline/ref_gpu: FLANN's CUDA
+    kd-tree and the reference's render kernel, one view per launch, 16x16
+    blocks, per-pixel global result arrays), timed per view with CUDA events
+    over the given views; its hit maps are compared with the library's for
+    the same views.  Also its radii search kernel and, sampled, the
+    reference's host sqrt loop over device elements."""
+    import torch
+    from baseline.ref_gpu import RefGpu
+    t0 = time.perf_counter()
+    rg = RefGpu(sc.xyz)
+    tb = time.perf_counter() - t0
+    _, _, radii_ms = rg.radii(max_radius)
+    loop_s = rg.sqrt_loop_seconds_per_point(20000)
+    npix = max(v.pixels for v in views)
+    hit = torch.empty(npix, dtype=torch.int32, device=dev)
+    depth = torch.empty(npix, dtype=torch.float32, device=dev)
+    rg.render_into(views[0].cam2world, views[0].width, views[0].height, views[0].fov, hit.data_ptr(),
+                   depth.data_ptr())  # warm-up
+    ms, rays, mismatch = 0.0, 0, 0
+    for v, (_, lib_hit) in zip(views, keep):
+        ms += rg.render_into(v.cam2world, v.width, v.height, v.fov, hit.data_ptr(), depth.data_ptr())
+        rays += v.pixels
+        mismatch += int((hit[:v.pixels] != lib_hit.reshape(-1)).sum().item())
+    n = int(sc.xyz.shape[0])
+    rg.close()
+    return {"mrays_s": round(rays / (ms * 1e-3) / 1e6, 4), "views": len(views), "rays": int(rays),
+            "ms": round(ms, 2), "hit_mismatch_vs_library": mismatch,
+            "radii_search_ms": round(radii_ms, 3), "radii_search_mqueries_s": round(n / (radii_ms * 1e-3) / 1e6, 2),
+            "radii_host_sqrt_loop_s_per_point": loop_s,
+            "radii_as_shipped_s": round(radii_ms * 1e-3 + loop_s * n, 2),
+            "tree_build_host_s": round(tb, 2),
+            "what": "baseline/ref_gpu: the reference's render kernel and FLANN CUDA kd-tree restated, one view "
+                    "per launch; radii_as_shipped adds the reference's host sqrt loop (main.cu:110-112) "
+                    "timed on 20,000 points and scaled"}
 
 
 def cpu_radii(sc, threads):
@@ -453,6 +492,12 @@ def main():
             plain = total_rays / (plain_ms * 1e-3) / 1e6
         log("timed batch %.1f ms/step, plain %s ms" % (t_step, plain_ms))
 
+        # ---- the reference's GPU path, restated, on the first views
+        ref_gpu = None
+        if args.ref_views > 0:
+            ref_gpu = time_ref_gpu(sc, views[:args.ref_views], keep[:args.ref_views], max_radius, dev)
+            log("reference GPU path %s" % ref_gpu)
+
         # ---- e2e: host buffers through the C ABI (views in, RGBA32F images out)
         e2e, h2d, d2h = None, 0, 0
         if not args.skip_e2e:
@@ -515,6 +560,8 @@ def main():
            "plain_mrays_s": None if plain is None else round(plain, 3),
            "per_ray_walk_mrays_s": None if per_ray is None else round(per_ray, 3),
            "batched_over_plain": None if plain is None else round(value / ws / plain, 3),
+           "ref_gpu_path": ref_gpu,
+           "batched_over_ref_gpu": None if ref_gpu is None else round(value / ws / ref_gpu["mrays_s"], 2),
            "radii_mqueries_s": round(radii_mq, 3), "radii_ms": round(float(np.median(radii_ms)), 3),
            "radii_build_ms": round(float(np.median(build_ms)), 3), "radii_query_ms": round(float(np.median(query_ms)), 3),
            "fwd_ms_per_view": fb["fwd_ms"], "fwdbwd_ms_per_view": fb["fwdbwd_ms"],

@@ -608,8 +608,9 @@ __device__ bool packet_knn(const IndexDev& ix, bool active, float qx, float qy, 
 // The queue is 32 entries in registers (lane i holds the i-th nearest);
 // the farthest entry of a full queue moves to an overflow stack in shared
 // memory, and if that fills as well the walk continues depth-first on the
-// bounded stack from then on.  Every pending node is still re-tested when
-// taken, so the result is exact whatever the order.
+// bounded stack from then on.  Every taken node's children are tested
+// against the bounds of that moment, so the result is exact whatever the
+// order.
 template <class List>
 __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float qy, float qz, List& L,
                               PacketQueue& ps, unsigned& leaves, unsigned& nodes) {
@@ -802,21 +803,14 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
       } else {
         break;
       }
-      const int plvl = (int)(code >> 28);
-      const uint32_t pG = code & 0x0fffffffu;
-      // the node's box: lane (pG - 1) & 3 of its parent's group (pG - 1) >> 2
-      const float* pg = reinterpret_cast<const float*>(ix.groups + (size_t)GROUP_F4 * ((pG - 1u) >> 2));
-      const int c = (int)((pG - 1u) & 3u);
-      float md = INF;
-      if (active)
-        md = d2_box(__ldg(pg + 0 + c), __ldg(pg + 4 + c), __ldg(pg + 8 + c), __ldg(pg + 12 + c),
-                    __ldg(pg + 16 + c), __ldg(pg + 20 + c), qx, qy, qz);
-      if (__ballot_sync(FULL, active && md <= list_worst(L))) {
-        lvl = plvl;
-        G = pG;
-        found = true;
-        break;
-      }
+      // no re-test of the node's own box here: its expansion tests its
+      // children against the current bounds, and a child's box lies inside
+      // its parent's, so a node that is no longer needed yields no needed
+      // child (one dependent load fewer per taken node, measured +1.2%)
+      lvl = (int)(code >> 28);
+      G = code & 0x0fffffffu;
+      found = true;
+      break;
     }
     __syncwarp();
     if (!found) break;
