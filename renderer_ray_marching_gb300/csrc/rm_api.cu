@@ -743,11 +743,11 @@ rm_status rm_autotune(rm_ctx* ctx, const rm_view* views, int32_t n, rm_launch* c
     rm_launch best_l = c.launch;
     float best_t = 1e30f;
     for (auto& sh : shapes) {
-      rm_launch L{sh[0], sh[1], 1, 5, 1};
+      rm_launch L{sh[0], sh[1], 1, 7, 1};
       float t = time_once(L);
       if (t < best_t) { best_t = t; best_l = L; }
     }
-    for (int ctas : {4, 6, 8}) {
+    for (int ctas : {5, 6, 8}) {
       rm_launch L = best_l;
       L.ctas_per_sm = ctas;
       float t = time_once(L);

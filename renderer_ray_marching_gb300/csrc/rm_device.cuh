@@ -797,6 +797,20 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
       } else if (osp > 0) {
         --osp;
         code = ps.over[osp];
+        // Entries on the overflow stack were the farthest of a full queue,
+        // and by the time they are taken the bounds have shrunk: about 89%
+        // of them are no longer needed (20M-point workload).  Unlike a
+        // queue entry (87% still needed when taken), such a node is worth
+        // re-testing before its expansion: its box is lane (G - 1) & 3 of
+        // its parent's group (about 14 fewer expansions per warp step, +1%).
+        const uint32_t pG = code & 0x0fffffffu;
+        const float* pg = reinterpret_cast<const float*>(ix.groups + (size_t)GROUP_F4 * ((pG - 1u) >> 2));
+        const int c = (int)((pG - 1u) & 3u);
+        float md = INF;
+        if (active)
+          md = d2_box(__ldg(pg + 0 + c), __ldg(pg + 4 + c), __ldg(pg + 8 + c), __ldg(pg + 12 + c),
+                      __ldg(pg + 16 + c), __ldg(pg + 20 + c), qx, qy, qz);
+        if (!__ballot_sync(FULL, active && md <= list_worst(L))) continue;
       } else if (fsp > 0) {
         --fsp;
         code = ps.code[PSTACK - 1 - fsp];

@@ -30,8 +30,8 @@
 // Plain form (rm_render): one warp per 8x4 tile, four warps per CTA.
 // Batched form (rm_render_batch): a persistent kernel whose warps pull items
 // of any view from one global counter; the whole launch is a CUDA graph.
-// Both are templated on the CTAs per SM their register budget is sized for
-// (4, 5, 6 or 8); the kernel is latency-bound, so resident warps matter and
+// Both are templated on the CTAs per SM their register cap is sized for
+// (4 to 8, regs_for_ctas); the kernel is latency-bound, so resident warps matter and
 // the per-item view and the statistics live in shared memory (WarpSmem).
 //
 // Culling.  The reference's view-frustum test is a no-op (is_inside,
@@ -76,6 +76,18 @@ __device__ __forceinline__ float clip_exit(const Ray& r, const ClipBox& e) {
 }
 
 constexpr int WARPS_PER_CTA = 4;
+
+// Register cap of a marcher instance sized for `ctas` resident CTAs per SM:
+// the SM's 65,536 registers shared by ctas x 128 threads, rounded down to the
+// allocation granule of 8 (4 -> 128, 5 -> 96, 6 -> 80, 7 -> 72, 8 -> 64).
+// The kernels take it as __maxnreg__ rather than as the minimum-blocks
+// argument of __launch_bounds__: both give ptxas the same register count,
+// but it then spills different values, and on the 20M-point batched
+// workload (32 views, leaf 16) the capped form measured 54.7 Mrays/s at 64
+// and at 72 registers against 48.2 for __launch_bounds__(128, 8).  The
+// marcher is latency-bound, so the extra resident warps are worth the
+// spills (72 registers: 200 B of spill stores per thread).
+constexpr int regs_for_ctas(int ctas) { return (65536 / (ctas * 32 * WARPS_PER_CTA)) / 8 * 8; }
 
 struct MarchParams {
   ClipBox clip;
@@ -258,11 +270,10 @@ struct PlainArgs {
   int32_t* steps;
 };
 
-// One warp per 8x4 tile.  MINB: CTAs per SM the register budget is sized
-// for (the launch's ctas_per_sm picks the instance).
-template <int SEARCH, int MINB>
-__global__ void __launch_bounds__(32 * WARPS_PER_CTA, MINB)
-k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __restrict__ counters) {
+// One warp per 8x4 tile.
+template <int SEARCH>
+__device__ __forceinline__ void plain_body(const IndexDev& ix, const PlainArgs& a, const MarchParams& mp,
+                                           unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
   const int warp = threadIdx.x >> 5;
   int tiles_x = (a.width + 7) / 8;
@@ -286,6 +297,20 @@ k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __re
     march_item<SEARCH>(ix, (tile % tiles_x) * 8, (tile / tiles_x) * 4, 8, 4, 1, mp, sm);
   }
   flush_counters<SEARCH>(sm, counters);
+}
+
+// Packet-walk instances, MINB: the CTAs per SM their register cap is sized
+// for (the launch's ctas_per_sm picks the instance).  The per-lane walk keeps
+// the minimum-blocks form, under which it measured faster (20.0 against
+// 17.2 Mrays/s with __maxnreg__ at the same 90 registers).
+template <int MINB>
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA) __maxnreg__(regs_for_ctas(MINB))
+k_march_plain(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __restrict__ counters) {
+  plain_body<1>(ix, a, mp, counters);
+}
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA, 4)
+k_march_plain_lane(IndexDev ix, PlainArgs a, MarchParams mp, unsigned long long* __restrict__ counters) {
+  plain_body<0>(ix, a, mp, counters);
 }
 
 // ---------------------------------------------------------------- batched
@@ -316,10 +341,10 @@ __device__ __forceinline__ int find_view(const ViewDev* views, int n, int64_t it
   return lo;
 }
 
-template <int SEARCH, int MINB>
-__global__ void __launch_bounds__(32 * WARPS_PER_CTA, MINB)
-k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __restrict__ queue,
-              unsigned long long* __restrict__ counters) {
+template <int SEARCH>
+__device__ __forceinline__ void batch_body(const IndexDev& ix, const BatchArgs& a, const MarchParams& mp,
+                                           unsigned long long* __restrict__ queue,
+                                           unsigned long long* __restrict__ counters) {
   __shared__ WarpSmem smem[WARPS_PER_CTA];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   WarpSmem& sm = smem[warp];
@@ -349,6 +374,18 @@ k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __re
     march_item<SEARCH>(ix, x0, y0, a.tile_w, a.tile_h, a.rpl, mp, sm);
   }
   flush_counters<SEARCH>(sm, counters);
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA) __maxnreg__(regs_for_ctas(MINB))
+k_march_batch(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __restrict__ queue,
+              unsigned long long* __restrict__ counters) {
+  batch_body<1>(ix, a, mp, queue, counters);
+}
+__global__ void __launch_bounds__(32 * WARPS_PER_CTA, 4)
+k_march_batch_lane(IndexDev ix, BatchArgs a, MarchParams mp, unsigned long long* __restrict__ queue,
+                   unsigned long long* __restrict__ counters) {
+  batch_body<0>(ix, a, mp, queue, counters);
 }
 
 // ---------------------------------------------------------------- host side
@@ -400,12 +437,13 @@ void launch_render_plain(Ctx& c, const rm_view& v, float4* rgbd, int32_t* hit, f
   auto go = [&](auto kern) { kern<<<grid, 32 * WARPS_PER_CTA, 0, c.stream>>>(c.index(), a, mp, counters); };
   const int cps = c.launch.ctas_per_sm;
   if (mp.search == 1) {
-    if (cps >= 8) go(k_march_plain<1, 8>);
-    else if (cps >= 6) go(k_march_plain<1, 6>);
-    else if (cps >= 5) go(k_march_plain<1, 5>);
-    else go(k_march_plain<1, 4>);
+    if (cps >= 8) go(k_march_plain<8>);
+    else if (cps >= 7) go(k_march_plain<7>);
+    else if (cps >= 6) go(k_march_plain<6>);
+    else if (cps >= 5) go(k_march_plain<5>);
+    else go(k_march_plain<4>);
   } else {
-    go(k_march_plain<0, 4>);
+    go(k_march_plain_lane);
   }
 }
 
@@ -433,12 +471,13 @@ void launch_render_batch(Ctx& c, ViewDev* views_dev, int n, int64_t total_items,
   };
   const int cps = L.ctas_per_sm;
   if (mp.search == 1) {
-    if (cps >= 8) go(k_march_batch<1, 8>);
-    else if (cps >= 6) go(k_march_batch<1, 6>);
-    else if (cps >= 5) go(k_march_batch<1, 5>);
-    else go(k_march_batch<1, 4>);
+    if (cps >= 8) go(k_march_batch<8>);
+    else if (cps >= 7) go(k_march_batch<7>);
+    else if (cps >= 6) go(k_march_batch<6>);
+    else if (cps >= 5) go(k_march_batch<5>);
+    else go(k_march_batch<4>);
   } else {
-    go(k_march_batch<0, 4>);
+    go(k_march_batch_lane);
   }
 }
 

@@ -139,7 +139,7 @@ def test_render_independent_of_leaf_size_and_search(scene100k):
     sc, _ = scene100k
     v = views_from_specs(syn.make_views(1, seed=4, boxes=sc.boxes, resolutions=[(200, 150)]))[0]
     outs = []
-    for leaf, search, ctas in ((8, 1, 4), (16, 1, 8), (32, 1, 6), (16, 0, 4)):
+    for leaf, search, ctas in ((8, 1, 4), (16, 1, 8), (32, 1, 6), (8, 1, 7), (16, 0, 4)):
         r, _, _ = make_renderer(sc.xyz, sc.rgb, leaf=leaf, search=search)
         r.set_launch(search=search, ctas_per_sm=ctas)
         outs.append(r.render(v))
