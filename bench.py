@@ -385,7 +385,7 @@ def main():
                                                              float(np.median(query_ms))))
 
         # ---- autotune on a subset of views
-        tune = r.get_launch() if args.no_autotune else r.autotune(views[:16])
+        tune = r.get_launch() if args.no_autotune else r.autotune(views[:32])
         log("launch %s" % tune)
 
         # ---- batched, device-resident

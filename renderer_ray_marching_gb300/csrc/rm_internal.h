@@ -103,7 +103,7 @@ struct Ctx {
   DevBuf frame_bufs;     // device outputs for host-side frames
   DevBuf queue;          // work-queue counters
 
-  rm_launch launch{8, 4, 1, 7, 1};
+  rm_launch launch{8, 4, 1, 8, 1};
   rm_stats stats{};
   // set by the allocation-free batch, whose counters live in its static
   // scratch: rm_get_stats then reports zeros instead of the counters and

@@ -248,7 +248,7 @@ class Renderer:
         self._check(self._lib.rm_render_batch(self._h, cviews, len(views), frames,
                                               _abi.RM_DEVICE if device else _abi.RM_HOST))
 
-    def set_launch(self, tile_w=8, tile_h=4, rays_per_lane=1, ctas_per_sm=7, search=1):
+    def set_launch(self, tile_w=8, tile_h=4, rays_per_lane=1, ctas_per_sm=8, search=1):
         L = _abi.RmLaunch(tile_w, tile_h, rays_per_lane, ctas_per_sm, search)
         self._check(self._lib.rm_set_launch(self._h, ctypes.byref(L)))
 
