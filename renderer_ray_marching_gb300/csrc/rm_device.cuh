@@ -160,22 +160,27 @@ __device__ __forceinline__ void klist_insert(KList<K>& L, float d, int32_t s, fl
   }
 }
 
-// The marcher's 10 nearest, kept sorted by (d2, cloud index) in registers
-// (empty slots (+inf, -1) last), so the bound is always d[KNN-1].
-// Insertions skip points already present, so the set can start from the
-// previous step's points (they are valid candidates: the search then prunes
-// with a finite bound from the first node and stays exact).  Radii are not
-// kept here; the step value reads them from the records.
+// The marcher's 10 nearest, kept sorted by d2 in registers (runs of equal
+// d2 put in cloud-index order by order() before they are read), with
+// placeholder entries (index -1) last, so the bound is always d[KNN-1].  A
+// step starts with restart(): ten placeholders one ulp above the largest
+// distance of the previous step's points at the new position (a valid
+// bound: those are ten real candidates), so the search prunes with a finite
+// bound from the first node and stays exact, and every point it keeps is
+// met once.  Radii are not kept here; the step value reads them from the
+// records.
 //
 // Cost.  An insertion is the hot divergent path of the packet walk (about
-// 80 per ray step at 20M points), so its common case touches no memory and
-// takes no branch: one equality scan over the distances, then one select
-// pass that slides the new entry into place, with all ten comparisons
-// independent of each other (a serial compare-and-swap chain would leave
-// the warp waiting on each result).  A
-// duplicate of a present point has the same record and query, hence the
-// same d2 bits, so the equality scan catches duplicates together with exact
-// distance ties; both go to the ordered path that compares cloud indices.
+// 30 per ray step at 20M points), so its common case touches no memory and
+// takes no branch: one select pass that slides the new entry into place,
+// with all ten comparisons independent of each other (a serial
+// compare-and-swap chain would leave the warp waiting on each result).
+// Exact d2 ties only matter when one of the tied entries is about to leave
+// the set; that case (the 9th and 10th entries equal) takes the ordered
+// path, which compares cloud indices.  An earlier form kept the previous
+// step's points in the set and re-sorted them; the walk then met each of
+// them a second time, and every insertion had to test for duplicates first
+// (that form was 6% slower, with 80 more bytes of spills at 64 registers).
 struct KSet {
   float d[KNN];
   int32_t s[KNN];   // sorted position, -1 = empty
@@ -190,30 +195,26 @@ struct KSet {
 
   __device__ __forceinline__ float worst() const { return d[KNN - 1]; }
 
-  // Candidate (dd, ss) with dd <= worst().
+  // Candidate (dd, ss) with dd <= worst().  Fast path: dd is strictly
+  // below the 10th entry, and the entry it pushes out (the 10th) is strictly
+  // above the 9th or a placeholder, so no tie decides what leaves the set;
+  // the new entry goes in by d2 alone, after any equal entries, and order()
+  // sorts equal entries by cloud index before the set is read.
   __device__ __forceinline__ void consider(float dd, int32_t ss, const int32_t* __restrict__ perm) {
-    bool eq = false;
+    if (dd < d[KNN - 1] && (d[KNN - 2] < d[KNN - 1] || s[KNN - 2] < 0)) {
 #pragma unroll
-    for (int j = 0; j < KNN; ++j) eq |= (d[j] == dd);
-    if (eq) {
-      consider_ordered(dd, ss, perm);
+      for (int j = KNN - 1; j > 0; --j) {
+        const bool g = d[j] > dd, gp = d[j - 1] > dd;
+        d[j] = g ? (gp ? d[j - 1] : dd) : d[j];
+        s[j] = g ? (gp ? s[j - 1] : ss) : s[j];
+      }
+      const bool g0 = d[0] > dd;
+      d[0] = g0 ? dd : d[0];
+      s[0] = g0 ? ss : s[0];
       return;
     }
-    // no entry at distance dd: order by d2 alone.  The list is sorted, so
-    // the predicates d[j] > dd are false then true; every slot takes its own
-    // entry, the new one, or its left neighbour's (no serial chain).  Each
-    // comparison is written where it is used: a form that first stored the
-    // ten predicates in a bool array gave wrong results on the GPU in one
-    // kernel although the same C++ is correct on the CPU.
-#pragma unroll
-    for (int j = KNN - 1; j > 0; --j) {
-      const bool g = d[j] > dd, gp = d[j - 1] > dd;
-      d[j] = g ? (gp ? d[j - 1] : dd) : d[j];
-      s[j] = g ? (gp ? s[j - 1] : ss) : s[j];
-    }
-    const bool g0 = d[0] > dd;
-    d[0] = g0 ? dd : d[0];
-    s[0] = g0 ? ss : s[0];
+    order(perm);
+    consider_ordered(dd, ss, perm);
   }
 
   // Equal distances present: skip a duplicate, else insert by (d2, cloud index).
@@ -224,7 +225,7 @@ struct KSet {
     if (dup) return;
 #pragma unroll
     for (int j = 0; j < KNN; ++j) {
-      if (s[j] < 0 || knn_before(dd, ss, d[j], s[j], perm)) {  // empty slots are last
+      if (s[j] < 0 || knn_before(dd, ss, d[j], s[j], perm)) {  // placeholders are last
         const float td = d[j];
         const int32_t ts = s[j];
         d[j] = dd;
@@ -235,46 +236,18 @@ struct KSet {
     }
   }
 
-  // (d, s) pairs a and b in order (a first) by d2; equal d2 is left for the
-  // tie pass below.
-  __device__ __forceinline__ void cas(int a, int b) {
-    const bool sw = d[b] < d[a];
-    const float da = d[a], db = d[b];
-    const int32_t sa = s[a], sb = s[b];
-    d[a] = sw ? db : da;
-    d[b] = sw ? da : db;
-    s[a] = sw ? sb : sa;
-    s[b] = sw ? sa : sb;
-  }
-
-  // Re-measure the ten points at the next step's position and re-sort:
-  // a 29-comparator network on d2, then, only if two finite distances are
-  // equal, an insertion pass by (d2, cloud index).
-  __device__ __forceinline__ void rewarm(const IndexDev& ix, float qx, float qy, float qz) {
-#pragma unroll
-    for (int j = 0; j < KNN; ++j) {
-      if (s[j] >= 0) d[j] = d2_point(__ldg(ix.rec + s[j]), qx, qy, qz);
-    }
-    static_assert(KNN == 10, "sorting network is for 10 entries");
-    cas(4, 9); cas(3, 8); cas(2, 7); cas(1, 6); cas(0, 5);
-    cas(1, 4); cas(6, 9); cas(0, 3); cas(5, 8);
-    cas(0, 2); cas(3, 6); cas(7, 9);
-    cas(0, 1); cas(2, 4); cas(5, 7); cas(8, 9);
-    cas(1, 2); cas(4, 6); cas(7, 8); cas(3, 5);
-    cas(2, 5); cas(6, 8); cas(1, 3); cas(4, 7);
-    cas(2, 3); cas(6, 7);
-    cas(3, 4); cas(5, 6);
-    cas(4, 5);
+  // Sorts runs of equal d2 by cloud index (an insertion pass, taken only
+  // when two adjacent real entries have equal d2).
+  __device__ __forceinline__ void order(const int32_t* __restrict__ perm) {
     bool tie = false;
 #pragma unroll
     for (int j = 0; j + 1 < KNN; ++j) tie |= (d[j] == d[j + 1] && s[j + 1] >= 0);
     if (tie) {
-      // insertion sort by (d2, cloud index); equal-d2 runs are short
 #pragma unroll
       for (int i = 1; i < KNN; ++i) {
 #pragma unroll
         for (int j = i; j > 0; --j) {
-          if (s[j] >= 0 && knn_before(d[j], s[j], d[j - 1], s[j - 1], ix.perm)) {
+          if (s[j] >= 0 && knn_before(d[j], s[j], d[j - 1], s[j - 1], perm)) {
             const float td = d[j];
             const int32_t ts = s[j];
             d[j] = d[j - 1];
@@ -284,6 +257,31 @@ struct KSet {
           }
         }
       }
+    }
+  }
+
+  // Start of a step.  The previous step's ten points, re-measured at the new
+  // position, are ten valid candidates, so the largest of their distances w
+  // bounds the new 10th distance.  The set restarts empty, with placeholder
+  // entries (index -1) one ulp above w: the walk prunes with that bound from
+  // its first node, and the real points it finds (the ten again among them)
+  // replace the placeholders.  Restarting empty, rather than keeping the ten
+  // in the set, means that no point is met twice in a walk, so the common
+  // insertion needs no duplicate test.
+  __device__ __forceinline__ void restart(const IndexDev& ix, float qx, float qy, float qz) {
+    float w = 0.0f;
+    bool full = true;
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      if (s[j] >= 0) w = fmaxf(w, d2_point(__ldg(ix.rec + s[j]), qx, qy, qz));
+      else full = false;
+    }
+    const float ph = (full && w < __int_as_float(0x7f800000)) ? __int_as_float(__float_as_int(w) + 1)
+                                                              : __int_as_float(0x7f800000);
+#pragma unroll
+    for (int j = 0; j < KNN; ++j) {
+      d[j] = ph;
+      s[j] = -1;
     }
   }
 

@@ -9,14 +9,15 @@
 // position, found by a warp packet traversal:
 //
 //   1. seed: every lane re-measures its previous step's 10 points at the new
-//      position (valid candidates, so its 10th distance is finite at once)
-//      and re-sorts them;
+//      position; the largest of those distances bounds the new 10th distance
+//      (they are valid candidates), so its set restarts with that finite
+//      bound (KSet::restart);
 //   2. the warp walks the tree once, as a unit (packet_knn): a node is
 //      expanded when its box lies within the current 10th distance of ANY
 //      active lane (one OR-reduction of 4-bit child votes), children are
-//      visited nearest-first for a leading lane, and pending nodes wait on a
-//      shared-memory stack so every pop is re-tested against the (shrinking)
-//      bounds of all lanes;
+//      visited nearest-first for a leading lane, and pending nodes wait in a
+//      priority queue keyed by the leading lane's box distance
+//      (packet_knn_bf);
 //   3. a leaf's records are staged once for the whole warp (broadcast
 //      loads) and every lane updates its own sorted set, so all lanes'
 //      bounds tighten while the walk goes on.
@@ -202,7 +203,7 @@ __device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int t
     float px = __fmaf_rn(R.dx[lane], t, R.ox[lane]);
     float py = __fmaf_rn(R.dy[lane], t, R.oy[lane]);
     float pz = __fmaf_rn(R.dz[lane], t, R.oz[lane]);
-    if (stepping) L.rewarm(ix, px, py, pz);
+    if (stepping) L.restart(ix, px, py, pz);
     if (SEARCH == 1) {
       // One packet: every stepping lane walks with the warp.  (A split into
       // a tight and a loose packet helped the depth-first walk; with the
@@ -221,6 +222,7 @@ __device__ void march_item(const IndexDev& ix, int x0, int y0, int tile_w, int t
     }
     if (stepping) {
       int32_t s;
+      L.order(ix.perm);
       float step = L.step_value(ix, &s);
       const int nsteps = R.nsteps[lane] + 1;
       R.nsteps[lane] = nsteps;
