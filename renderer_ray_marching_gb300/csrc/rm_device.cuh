@@ -676,10 +676,10 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
   };
   int lvl = 0;
   uint32_t G = 0;
-  unsigned budget = PACKET_NODE_BUDGET;
+  const unsigned nodes0 = nodes;
   while (true) {
     ++nodes;
-    if (--budget == 0) return false;  // self-check: a walk this long means a broken bound
+    if (nodes - nodes0 >= PACKET_NODE_BUDGET) return false;  // self-check: a walk this long means a broken bound
     const float4* g = ix.groups + (size_t)GROUP_F4 * G;
     float m0, m1, m2, m3;
     {
@@ -693,9 +693,50 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
     unsigned mine = 0;
     if (active) mine = (m0 <= w ? 1u : 0u) | (m1 <= w ? 2u : 0u) | (m2 <= w ? 4u : 0u) | (m3 <= w ? 8u : 0u);
     const unsigned needm = __reduce_or_sync(FULL, mine);
-    if (needm != 0) {
-      // visiting order (2 bits per position, nearest first for the leading
-      // lane); with one needed child any order will do
+    if (needm != 0 && lvl + 1 != ix.depth && !dfs) {
+      // Inner node, best-first.  Keys are the leading lane's box distances:
+      // the walk descends into the nearest needed child unless a queued node
+      // is nearer still, and queues the other needed children (the queue
+      // keeps them in key order, so no ordering network is needed here).
+      const uint32_t child0 = 4u * G + 1u;
+      const uint32_t lcode = (uint32_t)(lvl + 1) << 28;
+      if (!(needm & (needm - 1u))) {
+        // one child (about 35% of expansions): one shuffle
+        const int c = __ffs(needm) - 1;
+        const float kc = __shfl_sync(FULL, c == 0 ? m0 : c == 1 ? m1 : c == 2 ? m2 : m3, leader);
+        if (qn == 0 || kc <= __shfl_sync(FULL, qkey, 0)) {
+          lvl = lvl + 1;
+          G = child0 + (uint32_t)c;
+          continue;
+        }
+        qpush(kc, lcode | (child0 + (uint32_t)c));
+      } else {
+        const float k0 = __shfl_sync(FULL, m0, leader), k1 = __shfl_sync(FULL, m1, leader);
+        const float k2 = __shfl_sync(FULL, m2, leader), k3 = __shfl_sync(FULL, m3, leader);
+        const float e0 = (needm & 1u) ? k0 : INF, e1 = (needm & 2u) ? k1 : INF;
+        const float e2 = (needm & 4u) ? k2 : INF, e3 = (needm & 8u) ? k3 : INF;
+        const int c01 = e1 < e0 ? 1 : 0, c23 = e3 < e2 ? 3 : 2;
+        const float k01 = fminf(e0, e1), k23 = fminf(e2, e3);
+        const int cf = k23 < k01 ? c23 : c01;  // nearest needed child, ties to the lower index
+        const bool down = qn == 0 || fminf(k01, k23) <= __shfl_sync(FULL, qkey, 0);
+        const unsigned topush = down ? (needm & ~(1u << cf)) : needm;
+        if (topush & 1u) qpush(k0, lcode | child0);
+        if (topush & 2u) qpush(k1, lcode | (child0 + 1u));
+        if (topush & 4u) qpush(k2, lcode | (child0 + 2u));
+        if (topush & 8u) qpush(k3, lcode | (child0 + 3u));
+        if (down) {
+          if (sp + fsp > PSTACK) return false;
+          __syncwarp();
+          lvl = lvl + 1;
+          G = child0 + (uint32_t)cf;
+          continue;
+        }
+      }
+      if (sp + fsp > PSTACK) return false;
+    } else if (needm != 0) {
+      // Leaf level (its leaves are scanned now), or the depth-first fallback.
+      // Visiting order (2 bits per position, nearest first for the leading
+      // lane); with one needed child any order will do.
       unsigned order = 0xE4u;  // 0, 1, 2, 3
       if (needm & (needm - 1u)) {
         float k0 = m0, k1 = m1, k2 = m2, k3 = m3;
@@ -755,27 +796,6 @@ __device__ bool packet_knn_bf(const IndexDev& ix, bool active, float qx, float q
           __syncwarp();
           lvl = lvl + 1;
           G = child0 + ((order >> (2 * tf)) & 3u);
-          continue;
-        }
-        // best-first: keys are the leading lane's box distances; descend into
-        // the nearest child unless a queued node is nearer still
-        const float k0 = __shfl_sync(FULL, m0, leader), k1 = __shfl_sync(FULL, m1, leader);
-        const float k2 = __shfl_sync(FULL, m2, leader), k3 = __shfl_sync(FULL, m3, leader);
-        const int cf = (int)((order >> (2 * tf)) & 3u);
-        const float kf = cf == 0 ? k0 : cf == 1 ? k1 : cf == 2 ? k2 : k3;
-        const bool down = qn == 0 || kf <= __shfl_sync(FULL, qkey, 0);
-        const unsigned topush = down ? rest : om;
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          if (!((topush >> t) & 1u)) continue;
-          const int c = (int)((order >> (2 * t)) & 3u);
-          qpush(c == 0 ? k0 : c == 1 ? k1 : c == 2 ? k2 : k3, lcode | (child0 + (uint32_t)c));
-        }
-        if (sp + fsp > PSTACK) return false;
-        __syncwarp();
-        if (down) {
-          lvl = lvl + 1;
-          G = child0 + (uint32_t)cf;
           continue;
         }
       }
