@@ -110,7 +110,9 @@ typedef struct {
   int32_t tile_w;        /* warp tile width in pixels (tile_w * tile_h == 32) */
   int32_t tile_h;
   int32_t rays_per_lane; /* tiles per work item; a lane whose ray ends takes the item's next pixel */
-  int32_t ctas_per_sm;   /* persistent CTAs per SM (batched form) */
+  int32_t ctas_per_sm;   /* resident 4-warp CTAs per SM (1-16; the packet marchers have register-
+                            capped instances for 4-8: 128, 96, 80, 72 or 64 registers per
+                            thread; default 8) */
   int32_t search;        /* 1: the warp walks the index once for all its rays (packet
                             traversal, default); 0: every ray walks it alone */
 } rm_launch;
