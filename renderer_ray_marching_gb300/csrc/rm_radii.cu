@@ -32,7 +32,7 @@ k_radii(IndexDev ix, float max_radius, float* __restrict__ radii_out, int32_t* _
 
 // Packet form: a warp takes 32 consecutive sorted points (spatial
 // neighbours along the Morton curve), seeds each lane's 2-NN list with the
-// point itself and its next (or previous) record, and walks the tree once
+// point itself and its previous and next records, and walks the tree once
 // for all 32 (packet_knn).  Same results as k_radii.
 //
 // Memory traffic.  Warps take their 32-point chunks from a global counter
@@ -60,11 +60,18 @@ k_radii_packet(IndexDev ix, float* __restrict__ r_sorted, int32_t* __restrict__ 
     KList<2> L;
     klist_init<2>(L);
     if (active) {
+      // seeds: the point itself and both of its sorted neighbours.  The
+      // nearer neighbour bounds the search from its first node; the warp's
+      // walk is steered by its loosest lane, and a Morton jump on one side
+      // of a point rarely falls on the other (both seeds: -9% at 20M points)
       klist_insert<2>(L, d2_point(q, q.x, q.y, q.z), (int32_t)s, q.w, ix.perm);
-      int64_t nb = (s + 1 < ix.n) ? s + 1 : s - 1;
-      if (nb >= 0 && nb != s) {
-        float4 c = __ldg(ix.rec + nb);
-        klist_insert<2>(L, d2_point(c, q.x, q.y, q.z), (int32_t)nb, c.w, ix.perm);
+      if (s + 1 < ix.n) {
+        const float4 c = __ldg(ix.rec + s + 1);
+        klist_insert<2>(L, d2_point(c, q.x, q.y, q.z), (int32_t)(s + 1), c.w, ix.perm);
+      }
+      if (s >= 1) {
+        const float4 c = __ldg(ix.rec + s - 1);
+        list_consider_unique(L, d2_point(c, q.x, q.y, q.z), (int32_t)(s - 1), c.w, ix.perm);
       }
     }
     if (!packet_knn(ix, active, q.x, q.y, q.z, L, stacks[warp], leaves, nodes) && active) atomicAdd(err, 1ull);
