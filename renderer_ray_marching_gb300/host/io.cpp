@@ -529,17 +529,71 @@ void chunk(std::vector<unsigned char>& out, const char* type, const unsigned cha
 }
 }  // namespace
 
-void write_png(const std::string& path, int width, int height, int channels, const uint8_t* rows) {
+namespace {
+// One zlib stream (level 1) over `raw`, deflated in `slices` row-aligned
+// slices on as many threads: every slice is a raw deflate stream of its own
+// rows, the first ones ending on a sync flush (an empty stored block, so the
+// next slice starts byte-aligned) and the last one on the final block; the
+// stream's Adler-32 is combined from the slices' sums.  Each slice starts
+// without the previous one's history, which costs a little compression.
+std::vector<unsigned char> zlib_slices(const std::vector<unsigned char>& raw, size_t row_bytes, int slices) {
+  const size_t rows = raw.size() / row_bytes;
+  std::vector<std::vector<unsigned char>> part(slices);
+  std::vector<uLong> sum(slices);
+  std::vector<size_t> len(slices);
+  std::vector<int> ok(slices, 0);
+  std::vector<std::thread> workers;
+  for (int t = 0; t < slices; ++t)
+    workers.emplace_back([&, t] {
+      const size_t b = rows * t / slices * row_bytes, e = rows * (t + 1) / slices * row_bytes;
+      len[t] = e - b;
+      sum[t] = adler32(adler32(0L, Z_NULL, 0), raw.data() + b, (uInt)(e - b));
+      z_stream zs;
+      memset(&zs, 0, sizeof(zs));
+      if (deflateInit2(&zs, 1, Z_DEFLATED, -15, 8, Z_DEFAULT_STRATEGY) != Z_OK) return;
+      part[t].resize(deflateBound(&zs, (uLong)(e - b)) + 64);
+      zs.next_in = const_cast<unsigned char*>(raw.data() + b);
+      zs.avail_in = (uInt)(e - b);
+      zs.next_out = part[t].data();
+      zs.avail_out = (uInt)part[t].size();
+      const bool last = t == slices - 1;
+      const int rc = deflate(&zs, last ? Z_FINISH : Z_SYNC_FLUSH);
+      ok[t] = (last ? rc == Z_STREAM_END : rc == Z_OK) && zs.avail_in == 0;
+      part[t].resize(part[t].size() - zs.avail_out);
+      deflateEnd(&zs);
+    });
+  for (auto& w : workers) w.join();
+  std::vector<unsigned char> z = {0x78, 0x01};  // deflate, 32 KB window, fastest level
+  uLong a = sum[0];
+  for (int t = 0; t < slices; ++t) {
+    if (!ok[t]) throw std::runtime_error("PNG: deflate failed");
+    z.insert(z.end(), part[t].begin(), part[t].end());
+    if (t) a = adler32_combine(a, sum[t], (z_off_t)len[t]);
+  }
+  put32(z, (uint32_t)a);
+  return z;
+}
+}  // namespace
+
+void write_png(const std::string& path, int width, int height, int channels, const uint8_t* rows, int threads) {
   size_t row = (size_t)width * channels;
   std::vector<unsigned char> raw((row + 1) * height);
   for (int y = 0; y < height; ++y) {
     raw[y * (row + 1)] = 0;  // filter: none
     memcpy(&raw[y * (row + 1) + 1], rows + (size_t)y * row, row);
   }
-  uLongf zlen = compressBound((uLong)raw.size());
-  std::vector<unsigned char> z(zlen);
-  if (compress2(z.data(), &zlen, raw.data(), (uLong)raw.size(), 1) != Z_OK)
-    throw std::runtime_error("PNG: deflate failed");
+  std::vector<unsigned char> z;
+  uLongf zlen = 0;
+  const int slices = (int)std::min<size_t>((size_t)std::max(threads, 1), (size_t)height);
+  if (slices > 1 && raw.size() >= ((size_t)1 << 20) && raw.size() / slices < ((size_t)1 << 30)) {
+    z = zlib_slices(raw, row + 1, slices);
+    zlen = (uLongf)z.size();
+  } else {
+    zlen = compressBound((uLong)raw.size());
+    z.resize(zlen);
+    if (compress2(z.data(), &zlen, raw.data(), (uLong)raw.size(), 1) != Z_OK)
+      throw std::runtime_error("PNG: deflate failed");
+  }
   std::vector<unsigned char> out = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
   unsigned char ihdr[13];
   uint32_t w = (uint32_t)width, h = (uint32_t)height;

@@ -52,8 +52,12 @@ Json load_json(const std::string& path);
 void json_mat4(const Json& j, float out[16]);
 
 // PNG writers (zlib-compressed, 8-bit).  Rows are written top-down from
-// `rows`, which callers pass already flipped.
-void write_png(const std::string& path, int width, int height, int channels, const uint8_t* rows);
+// `rows`, which callers pass already flipped.  With threads > 1 an image of
+// at least 1 MB is deflated in that many row slices at once (one zlib
+// stream: each slice ends on a byte-aligned flush and the slices' Adler-32
+// sums are combined), so the decoded pixels are the same.
+void write_png(const std::string& path, int width, int height, int channels, const uint8_t* rows,
+               int threads = 1);
 // float32 (H, W) C-order .npy
 void write_npy_f32(const std::string& path, int height, int width, const float* data);
 

@@ -136,16 +136,19 @@ struct Pending {
   std::unique_ptr<FileLock> lock;
 };
 
-void save_outputs(const Pending& p, const std::vector<float>& rgbd) {
+// Writes one view's files.  `threads`: how many row slices each PNG is
+// deflated in at once (the per-view mode gives one view all host cores; the
+// batch mode already writes several views at a time, one core each).
+void save_outputs(const Pending& p, const std::vector<float>& rgbd, int threads) {
   int w = p.view.width, h = p.view.height;
   std::vector<uint8_t> png;
   rmio::encode_colour_rgba8(w, h, rgbd.data(), png);
-  rmio::write_png(p.out.string(), w, h, 4, png.data());
+  rmio::write_png(p.out.string(), w, h, 4, png.data(), threads);
   std::vector<uint8_t> dpng;
   std::vector<float> depth;
   rmio::encode_depth_u8(w, h, rgbd.data(), dpng, depth);
   rmio::write_npy_f32(p.depth_out.string() + ".npy", h, w, depth.data());
-  rmio::write_png(p.depth_out.string(), w, h, 1, dpng.data());
+  rmio::write_png(p.depth_out.string(), w, h, 1, dpng.data(), threads);
 }
 
 int run(const Args& a) {
@@ -273,8 +276,10 @@ int run(const Args& a) {
     pending.push_back(std::move(p));
   };
 
+  const unsigned hw_threads = std::thread::hardware_concurrency();
+  const int view_threads = (int)std::min(hw_threads ? hw_threads : 1u, 16u);
   auto finish = [&](Pending& p, const std::vector<float>& rgbd, double secs) {
-    save_outputs(p, rgbd);
+    save_outputs(p, rgbd, view_threads);
     cout << fs::canonical(fs::absolute(p.out)) << ": " << (float)secs << " s" << endl;
     p.lock->unlock();
     fs::remove(p.lock_path);
@@ -332,7 +337,7 @@ int run(const Args& a) {
       workers.emplace_back([&, w] {
         for (size_t i = w; i < nv; i += nt) {
           try {
-            save_outputs(pending[i], images[i]);
+            save_outputs(pending[i], images[i], 1);
           } catch (...) {
             err[i] = std::current_exception();
           }

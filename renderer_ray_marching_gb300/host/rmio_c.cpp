@@ -2,8 +2,10 @@
 // formats of the reference's process boundary can be used and tested
 // without a GPU.  Every function returns 0 on success, -1 on failure with
 // the message available from rmio_last_error() (per thread).
+#include <algorithm>
 #include <cstring>
 #include <string>
+#include <thread>
 
 #include "io.hpp"
 #include "rmio.h"
@@ -76,11 +78,13 @@ int rmio_write_frame(const char* colour_png, const char* depth_png, int32_t widt
   return guarded([&] {
     std::vector<uint8_t> png, dpng;
     std::vector<float> depth;
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int threads = (int)std::min(hw ? hw : 1u, 16u);  // one frame: its PNGs deflate in row slices
     rmio::encode_colour_rgba8(width, height, rgbd, png);
-    rmio::write_png(colour_png, width, height, 4, png.data());
+    rmio::write_png(colour_png, width, height, 4, png.data(), threads);
     rmio::encode_depth_u8(width, height, rgbd, dpng, depth);
     rmio::write_npy_f32(std::string(depth_png) + ".npy", height, width, depth.data());
-    rmio::write_png(depth_png, width, height, 1, dpng.data());
+    rmio::write_png(depth_png, width, height, 1, dpng.data(), threads);
   });
 }
 

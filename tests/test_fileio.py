@@ -1,4 +1,6 @@
 """Host file formats of the reference's process boundary, on CPU."""
+import os
+
 import numpy as np
 import pytest
 
@@ -97,6 +99,34 @@ def test_frame_encoders(tmp_path):
     assert np.array_equal(dep, ref)
     npy = np.load(d + ".npy")
     assert npy.dtype == np.float32 and npy.shape == (h, w) and np.array_equal(npy, v)
+
+
+def test_large_frame_pngs_deflated_in_slices(tmp_path):
+    """A frame of 1920x1080 is deflated in row slices on several threads (one
+    zlib stream: slices end on a sync flush, Adler-32 sums combined); the
+    standard decoder (which checks the stream's checksum) gives the same
+    pixels, and the stream holds more than one deflate segment."""
+    h, w = 1080, 1920
+    rng = np.random.default_rng(5)
+    rgbd = np.zeros((h, w, 4), np.float32)
+    rgbd[..., :3] = rng.integers(0, 4, size=(h, w, 3)).astype(np.float32) / np.float32(3.0)  # compressible
+    rgbd[..., 3] = rng.random((h, w)).astype(np.float32) * np.float32(90.0)
+    rgbd[: h // 3, :, 3] = 0.0
+    c, d = str(tmp_path / "big_color.png"), str(tmp_path / "big_depth.png")
+    fileio.write_frame(c, d, rgbd)
+    col = read_png(c)
+    flipped = rgbd[::-1]
+    assert np.array_equal(col[..., :3], (flipped[..., :3] * np.float32(255.0)).astype(np.uint8))
+    assert np.all(col[..., 3] == 255)
+    dep = read_png(d)
+    v = flipped[..., 3]
+    ref = np.clip(np.float32(2.55) * v, 0, 255).astype(np.uint8)
+    ref[np.abs(v - np.float32(1.0)) < np.float32(1e-5)] = 0
+    assert np.array_equal(dep, ref)
+    if (os.cpu_count() or 1) > 1:
+        # a sync flush leaves an empty stored block (00 00 ff ff) between slices
+        data = open(c, "rb").read()
+        assert b"\x00\x00\xff\xff" in data
 
 
 def test_json_rows_become_columns():
